@@ -1,0 +1,409 @@
+"""Benchmark: device malloc+free throughput of the GB300 ScatterAlloc heap.
+
+Workload (the full-GPU uniform stress): an 8 GiB heap (pagesize 4096, the
+reference's default 2 GiB access blocks, regionsize 16, wastefactor 2,
+XMallocSIMD, ReturnNull, Shrink<16>); grid = SMs x 8 blocks x 256 threads;
+every thread runs 100 rounds of {malloc(size), write a u64 pattern, verify it,
+free}; sizes uniform in {16, 32, ..., 1024}, drawn from a seeded SplitMix64
+table (synthetic). One step = one launch over the whole grid.
+
+  value  pairs/s with the size table resident in HBM (kernel time, CUDA events)
+  e2e    pairs/s through the C ABI with host buffers: H2D of the step's size
+         table from pinned memory + kernel + D2H of the result counters
+  roofline         HBM roofline of the stress kernel (payload + metadata bytes)
+  atomic_roofline  L2 atomic ops/s against a measured atomicOr peak
+  cpu_baseline     the oracle port of the reference's CPU backend on the host cores
+
+`--impl reference` times the reference's CPU implementation of the path (the
+oracle port) on the host cores instead.
+Multi-GPU: replicas only (each rank owns an independent heap).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "malloc+free ops/s on 1 GB300 (batched vs plain launch); p99 serve latency"
+UNIT = "malloc+free pairs/s"
+SEED = 20261203
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--heap-gib", type=float, default=8.0)
+    ap.add_argument("--rounds", type=int, default=100)
+    ap.add_argument("--blocks-per-sm", type=int, default=8)
+    ap.add_argument("--threads", type=int, default=256)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-peak", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target length of the CPU baseline sample")
+    return ap.parse_args()
+
+
+def size_table(rounds: int, nthreads: int, seed: int = SEED) -> np.ndarray:
+    """u16 [rounds, nthreads]: 16 * (1 + mix64(seed, t, r) % 64)."""
+    from oracle.oracle import mix64
+
+    t = np.arange(nthreads, dtype=np.uint64)
+    out = np.empty((rounds, nthreads), dtype=np.uint16)
+    for r in range(rounds):
+        out[r] = (16 * (1 + (mix64(seed, t, r) % np.uint64(64)))).astype(np.uint16)
+    return out
+
+
+def algorithmic_work(sizes: np.ndarray, pagesize: int = 4096):
+    """Minimum global atomics and bytes per launch under the reference algorithm.
+
+    Per (warp, round): lanes with size < pagesize/32 coalesce (XMallocSIMD) when
+    there are at least two: one chunk of 16 + sum, malloc 3 atomics (CAS
+    chunksize, add count, or mask), free k refcount subtractions + 3 (hierarchical
+    chunk) or + 2; every other lane: 3 + 3 or 3 + 2. Hierarchical iff chunk <= (P-8)/33.
+    Bytes: payload written and read back (2 x size) + 4 B per atomic + 16 B of
+    metadata reads per pair (chunksize on free, region counter, first-free-block,
+    segment mask)."""
+    ht = (pagesize - 8) // 33
+    s = sizes.astype(np.int64)
+    R, T = s.shape
+    w = s[:, : (T // 32) * 32].reshape(R, -1, 32)
+    co = w < pagesize // 32
+    k = co.sum(axis=2)
+    csum = np.where(co, w, 0).sum(axis=2)
+    grp = k >= 2
+    chunk_g = 16 + csum
+    atom_g = np.where(grp, 3 + np.where(chunk_g <= ht, 3, 2) + k, 0)
+    single = ~(co & grp[:, :, None])
+    c1 = np.maximum(w, 16)
+    atom_s = np.where(single, 3 + np.where(c1 <= ht, 3, 2), 0).sum(axis=2)
+    atomics = int(atom_g.sum() + atom_s.sum())
+    pairs = int(s.size)
+    payload = int(2 * s.sum())
+    meta = 4 * atomics + 16 * pairs
+    return {"pairs": pairs, "atomics": atomics, "atomics_per_pair": atomics / pairs, "payload_bytes": payload,
+            "metadata_bytes": meta, "bytes": payload + meta}
+
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region (clocks and throttle reasons)."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except FileNotFoundError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[3:7]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return d, "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def atomic_peak(torch, sms):
+    """Measured relaxed device-scope atomicOr throughput (ops/s)."""
+    from mallocmc_gb300.workloads import atomic_peak as launch
+
+    res = {}
+    sink = torch.zeros(1, dtype=torch.int64, device="cuda")
+    blocks, tpb, iters = sms * 8, 256, 512
+    for name, words, returning, contended in (("atom_l2_32MiB", 8 << 20, True, False),
+                                              ("red_l2_32MiB", 8 << 20, False, False),
+                                              ("atom_hbm_4GiB", 1 << 30, True, False),
+                                              ("atom_warp_same_word", 8 << 20, True, True)):
+        buf = torch.zeros(words, dtype=torch.int32, device="cuda")
+        s = torch.cuda.current_stream()
+        for _ in range(2):
+            launch(buf.data_ptr(), words, blocks, tpb, iters, returning, contended, sink.data_ptr())
+        torch.cuda.synchronize()
+        best = 0.0
+        for _ in range(5):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(s)
+            launch(buf.data_ptr(), words, blocks, tpb, iters, returning, contended, sink.data_ptr())
+            e1.record(s)
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1)
+            best = max(best, blocks * tpb * iters / (ms * 1e-3))
+        res[name] = best
+        del buf
+    torch.cuda.empty_cache()
+    return res
+
+
+def cpu_port_run(heap_gib, threads_total, rounds, target_s, workers):
+    """The oracle port of the reference's CPU backend on `workers` host threads,
+    on a bounded sample (virtual threads x rounds) of the same workload."""
+    from oracle.oracle import HeapConfig, OracleHeap
+
+    cfg = HeapConfig(4096, 2 << 30, 16, 2, False)
+    heap = OracleHeap(cfg, int(heap_gib * (1 << 30)))
+    cal = heap.run_stress(4096, 4, SEED, 16, 1024, 16, workers)
+    rate = cal["pairs"] / max(cal["seconds"], 1e-6)
+    vthreads = int(min(threads_total, max(1024, target_s * rate / rounds)))
+    r = heap.run_stress(vthreads, rounds, SEED + 1, 16, 1024, 16, workers)
+    heap.close()
+    return r, vthreads
+
+
+def reference_arm(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    workers = os.cpu_count() or 1
+    threads_total = 152 * args.blocks_per_sm * args.threads
+    per_step_s = 2.0
+    heap_gib = args.heap_gib
+    try:
+        from oracle.oracle import lib as olib
+
+        olib()
+    except Exception:
+        subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "liboracle.so"], check=True, capture_output=True)
+    vals, samples = [], None
+    for i in range(args.warmup + args.steps):
+        try:
+            r, vt = cpu_port_run(heap_gib, threads_total, args.rounds, per_step_s, workers)
+        except ValueError:
+            heap_gib = 1.0
+            r, vt = cpu_port_run(heap_gib, threads_total, args.rounds, per_step_s, workers)
+        if i >= args.warmup:
+            vals.append(r["pairs"] / r["seconds"])
+            samples = (vt, r)
+    v = float(statistics.median(vals))
+    vt, r = samples
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * r["seconds"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u32", "data": "synthetic (seeded SplitMix64 size draws)",
+        "config": {"workload": "uniform_stress", "heap_bytes": int(heap_gib * (1 << 30)), "rounds": args.rounds,
+                   "sizes": "uniform {16,32,...,1024}",
+                   "policies": "Scatter<4096,2GiB,16,2,noreset>+XMallocSIMD+ReturnNull+Shrink<16>"},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": workers, "kind": "port",
+                         "sample": f"{vt} virtual threads x {args.rounds} rounds per step (alpaka CPU-backend "
+                                   f"semantics: warp size 1, smid = warpid = 0) on {workers} host threads"},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "errors": {"nulls": r["nulls"], "pattern": r["bad"]},
+    }
+    print(json.dumps(line))
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        reference_arm(args)
+        return
+    import torch
+
+    from mallocmc_gb300 import AlignmentPolicies, Allocator, CreationPolicies, DistributionPolicies, _lib
+    from mallocmc_gb300.workloads import launch_stress, stress_params
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if not os.path.exists(_lib.LIB_PATH):
+        import __graft_entry__
+
+        __graft_entry__.build()
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    props = torch.cuda.get_device_properties(local)
+    sms = props.multi_processor_count
+    blocks = sms * args.blocks_per_sm
+    tpb = args.threads
+    nthreads = blocks * tpb
+    rounds = args.rounds
+    heap_bytes = int(args.heap_gib * (1 << 30))
+
+    sizes_np = size_table(rounds, nthreads)
+    work = algorithmic_work(sizes_np)
+    creation = CreationPolicies.Scatter(pagesize=4096, accessblocksize=2 << 30, regionsize=16, wastefactor=2)
+    alloc = Allocator(creation, DistributionPolicies.XMallocSIMD(4096), None, None, AlignmentPolicies.Shrink(16),
+                      size=heap_bytes, device=local)
+    stream = torch.cuda.current_stream()
+    h_sizes = torch.from_numpy(sizes_np.view(np.int16)).pin_memory()
+    d_sizes = h_sizes.to("cuda", non_blocking=False)
+    stats = torch.zeros(4, dtype=torch.int64, device="cuda")
+    h_stats = torch.zeros(4, dtype=torch.int64).pin_memory()
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
+    params = stress_params(blocks, tpb, rounds, 16, 1024, 16, SEED, True)
+
+    def step(sizes_ptr):
+        launch_stress(alloc, params, sizes_ptr, stats.data_ptr(), stream)
+
+    for _ in range(max(3, args.warmup)):
+        stats.zero_()
+        step(d_sizes.data_ptr())
+    torch.cuda.synchronize()
+    if int(stats[1].item()) or int(stats[2].item()):
+        raise RuntimeError(f"warm-up step reported nulls/pattern errors: {stats.tolist()}")
+
+    # ---- value: size table resident in HBM, kernel time only ----
+    stats.zero_()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    with ClockSampler(local) as clk:
+        t0 = time.perf_counter()
+        for e0, e1 in evs:
+            flush.zero_()  # L2 flush (512 MiB write) between timed steps, outside the events
+            e0.record(stream)
+            step(d_sizes.data_ptr())
+            e1.record(stream)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    if dist:
+        dist.barrier()
+    ms = [e0.elapsed_time(e1) for e0, e1 in evs]
+    st = stats.cpu().numpy().view(np.uint64)
+    if int(st[0]) != work["pairs"] * args.steps or int(st[1]) or int(st[2]):
+        raise RuntimeError(f"timed steps failed verification: {st.tolist()}")
+    total_ms = float(sum(ms))
+    if dist:
+        t = torch.tensor([total_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    per_step_ms = total_ms / args.steps
+    value = work["pairs"] * world / (per_step_ms * 1e-3)
+
+    # ---- e2e: through the C ABI with host buffers ----
+    e2e = None
+    if not args.no_e2e:
+        evs2 = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+        torch.cuda.synchronize()
+        for e0, e1 in evs2:
+            flush.zero_()
+            stats.zero_()
+            e0.record(stream)
+            d_sizes.copy_(h_sizes, non_blocking=True)
+            step(d_sizes.data_ptr())
+            h_stats.copy_(stats, non_blocking=True)
+            e1.record(stream)
+        torch.cuda.synchronize()
+        e2e_ms = sum(e0.elapsed_time(e1) for e0, e1 in evs2) / args.steps
+        if dist:
+            t = torch.tensor([e2e_ms], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            e2e_ms = float(t.item())
+        e2e = {"value": work["pairs"] * world / (e2e_ms * 1e-3), "unit": UNIT,
+               "h2d_bytes_per_step": int(sizes_np.nbytes), "d2h_bytes_per_step": int(h_stats.numel() * 8),
+               "ms_per_step": e2e_ms}
+
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return
+
+    peaks, peak_kind = measured_peaks()
+    kernel_s = per_step_ms * 1e-3
+    achieved_gbs = work["bytes"] / kernel_s / 1e9
+    roofline = {"bound": "hbm", "achieved": achieved_gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                "frac": achieved_gbs / peaks["hbm_gbs"], "traffic": None, "peak_kind": peak_kind,
+                "algorithmic_bytes_per_launch": work["bytes"], "payload_bytes_per_launch": work["payload_bytes"],
+                "metadata_bytes_per_launch": work["metadata_bytes"], "kernel": "mmc_stress_kernel"}
+    atomic = None
+    if not args.no_peak:
+        pk = atomic_peak(torch, sms)
+        ach = work["atomics"] / kernel_s
+        atomic = {"bound": "l2_atomic", "achieved": ach / 1e9, "peak": pk["atom_l2_32MiB"] / 1e9, "unit": "Gatomic/s",
+                  "frac": ach / pk["atom_l2_32MiB"], "atomics_per_pair": work["atomics_per_pair"],
+                  "peaks_measured_gops": {k: v / 1e9 for k, v in pk.items()}}
+    cpu = None
+    if not args.no_cpu_baseline:
+        workers = os.cpu_count() or 1
+        try:
+            r, vt = cpu_port_run(args.heap_gib, nthreads, rounds, args.cpu_seconds, workers)
+        except ValueError:
+            r, vt = cpu_port_run(1.0, nthreads, rounds, args.cpu_seconds, workers)
+        cpu = {"value": r["pairs"] / r["seconds"], "unit": UNIT, "cores": workers, "kind": "port",
+               "sample": f"{vt} virtual threads x {rounds} rounds (alpaka CPU-backend semantics) on {workers} host "
+                         f"threads, {r['seconds']:.1f} s"}
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": per_step_ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+        "data": "synthetic (seeded SplitMix64 size draws)",
+        "config": {"workload": f"uniform_stress_{args.heap_gib:g}GiB", "heap_bytes": heap_bytes,
+                   "grid": f"{sms}x{args.blocks_per_sm} blocks x {tpb} threads", "rounds": rounds,
+                   "sizes": "uniform {16,32,...,1024} (u16 table in HBM)",
+                   "policies": "Scatter<4096,2GiB,16,2,noreset>+XMallocSIMD+ReturnNull+Shrink<16>",
+                   "pairs_per_step": work["pairs"], "l2": "flushed between timed steps (512 MiB write)",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "roofline": roofline, "atomic_roofline": atomic, "cpu_baseline": cpu, "e2e": e2e,
+        "gpu_launches": args.steps, "clocks": clk.summary(), "wall_s_timed": wall,
+        "per_step_ms": ms,
+    }
+    print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,783 @@
+/* scatter_device.cuh — device side of the GB300 ScatterAlloc heap.
+ *
+ * Header-only __device__ code: user kernels include it (directly or through
+ * <mallocMC/mallocMC.hpp>) and call malloc/free/getAvailableSlots inline, as
+ * with the reference's AllocatorHandleImpl (mallocMC_allocator_handle.hpp:35-63).
+ * The algorithm is the reference's ScatterAlloc
+ * (src/include/mallocMC/creationPolicies/Scatter.hpp); every function cites the
+ * lines it follows. What is GB300-specific:
+ *   - the handle carries every immutable heap field by value (kernel parameter
+ *     space), so only the mutable words are read from memory;
+ *   - the page-table entries are three word arrays (chunksize[], count[],
+ *     bitmask[]) instead of an array of 12-byte structs: same bytes, same
+ *     numpages, but scans read only the words they need, fully coalesced;
+ *   - relaxed device-scope atomics (atom/red .relaxed.gpu) on L2-resident words
+ *     and ld.relaxed.gpu for the racy metadata reads;
+ *   - XMallocSIMD's warp coalescing uses __ballot_sync/__shfl_sync over the
+ *     lanes that are active at the call, not shared-memory counters;
+ *   - every spin is bounded: the page-based mutex gives up after a fixed
+ *     number of backed-off tries, records MMC_DEVERR_TIMEOUT and returns NULL;
+ *     the bit-claim retry loop gives up after MMC_USESPOT_MAX_TRIES.
+ * Thread-id sources are a template parameter: GpuIds reads %laneid/%warpid/
+ * %smid (mallocMC_utils.hpp:91-150); SerialIds is the reference CPU backend
+ * (all zero, warp size 1), which makes one device thread reproduce the
+ * reference's CPU-serial allocation sequence bit for bit.
+ */
+#pragma once
+
+#include "../mallocmc_gb300.h"
+
+#include <cstdint>
+
+#ifndef MMC_USESPOT_MAX_TRIES
+#define MMC_USESPOT_MAX_TRIES 256u
+#endif
+#ifndef MMC_MUTEX_MAX_SPINS
+#define MMC_MUTEX_MAX_SPINS (1u << 22)
+#endif
+
+/* Mutable heap words, each on its own 128-byte line. */
+struct mmc_heap_state
+{
+    uint32_t pagebasedMutex; /* Scatter.hpp:269 */
+    uint32_t pad0[31];
+    uint32_t firstFreePageBased; /* Scatter.hpp:270 */
+    uint32_t pad1[31];
+    uint32_t firstfreeblock; /* Scatter.hpp:271 */
+    uint32_t pad2[31];
+    uint32_t error_flags; /* MMC_DEVERR_* */
+    uint32_t pad3[31];
+};
+
+namespace mmc
+{
+    namespace dev
+    {
+        using u32 = uint32_t;
+        using u64 = uint64_t;
+
+        /* ---------------------------------------------------------- thread ids */
+        struct GpuIds
+        {
+            static constexpr u32 warpSize = 32u; /* mallocMC_utils.hpp:72-73 */
+            static constexpr bool coalesce = true;
+            __device__ static __forceinline__ u32 laneid()
+            {
+                u32 r;
+                asm volatile("mov.u32 %0, %%laneid;" : "=r"(r));
+                return r;
+            }
+            __device__ static __forceinline__ u32 warpid()
+            {
+                u32 r;
+                asm volatile("mov.u32 %0, %%warpid;" : "=r"(r));
+                return r;
+            }
+            __device__ static __forceinline__ u32 smid()
+            {
+                u32 r;
+                asm volatile("mov.u32 %0, %%smid;" : "=r"(r));
+                return r;
+            }
+        };
+
+        /* The reference's CPU-backend semantics (mallocMC_utils.hpp:85-87, 99-101, 121-123, 134-136). */
+        struct SerialIds
+        {
+            static constexpr u32 warpSize = 1u;
+            static constexpr bool coalesce = false; /* XMallocSIMD.hpp:136-137 */
+            __device__ static __forceinline__ u32 laneid() { return 0u; }
+            __device__ static __forceinline__ u32 warpid() { return 0u; }
+            __device__ static __forceinline__ u32 smid() { return 0u; }
+        };
+
+        /* ---------------------------------------------------- memory helpers */
+        __device__ __forceinline__ u32 ld_rlx(const u32* p)
+        {
+            u32 v;
+            asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+            return v;
+        }
+        __device__ __forceinline__ void st_rlx(u32* p, u32 v)
+        {
+            asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+        }
+        __device__ __forceinline__ u32 lanemask_lt()
+        {
+            u32 r;
+            asm("mov.u32 %0, %%lanemask_lt;" : "=r"(r));
+            return r;
+        }
+        __device__ __forceinline__ u32 umin(u32 a, u32 b) { return a < b ? a : b; }
+        __device__ __forceinline__ u32 umax(u32 a, u32 b) { return a > b ? a : b; }
+        __device__ __forceinline__ u32 divup(u32 a, u32 b) { return (a + b - 1u) / b; }
+
+        /* Shrink::applyPadding (Shrink.hpp:132-137) / Noop (alignmentPolicies/Noop.hpp:55-59). */
+        __host__ __device__ __forceinline__ u32 apply_padding(u32 align, u32 bytes)
+        {
+            if(align <= 1u)
+                return bytes;
+            const u32 clear = align - 1u;
+            return (bytes + clear) & ~clear;
+        }
+
+        __device__ __forceinline__ char* page_data(const mmc_device_handle& h, u32 page)
+        {
+            return h.pages + static_cast<u64>(page) * h.pagesize;
+        }
+
+        /* onPageMasksPosition, Scatter.hpp:315-318 */
+        __device__ __forceinline__ u32* on_page_masks(const mmc_device_handle& h, u32 page, u32 nMasks)
+        {
+            return reinterpret_cast<u32*>(page_data(h, page) + h.pagesize - 4u * nMasks);
+        }
+
+        /* Page::init, Scatter.hpp:247-258: zero the words that can hold on-page masks. */
+        __device__ __forceinline__ void page_init(const mmc_device_handle& h, u32 page)
+        {
+            u32* w = on_page_masks(h, page, h.maxOnPageMasks);
+            for(u32 i = 0; i < h.maxOnPageMasks; ++i)
+                st_rlx(w + i, 0u);
+        }
+
+        __device__ __forceinline__ void set_error(const mmc_device_handle& h, u32 bits)
+        {
+            atomicOr(&h.state->error_flags, bits);
+        }
+
+        /* nextspot, Scatter.hpp:293-304 */
+        __device__ __forceinline__ u32 nextspot(u32 bitfield, u32 spot, u32 spots)
+        {
+            const u32 low_part = (spot + 1u) == 32u ? 0u : (bitfield >> (spot + 1u));
+            const u32 high_part = (bitfield << (spots - (spot + 1u)));
+            const u32 selection_mask = spots == 32u ? ~0u : ((1u << spots) - 1u);
+            bitfield = (high_part | low_part) & selection_mask;
+            const u32 step = static_cast<u32>(__ffs(static_cast<int>(~bitfield)));
+            return (spot + step) % spots;
+        }
+
+        /* usespot, Scatter.hpp:329-347 (start at laneid % spots, randInit :277-281),
+         * with a retry bound: after MMC_USESPOT_MAX_TRIES lost races the word
+         * is reported full, which the callers already handle. */
+        template<class Ids>
+        __device__ __forceinline__ int usespot(u32* bitfield, u32 spots)
+        {
+            u32 spot = Ids::laneid() % spots;
+            for(u32 it = 0; it < MMC_USESPOT_MAX_TRIES; ++it)
+            {
+                const u32 mask = 1u << spot;
+                const u32 old = atomicOr(bitfield, mask);
+                if((old & mask) == 0u)
+                    return static_cast<int>(spot);
+                if(static_cast<u32>(__popc(old)) >= spots)
+                    return -1;
+                spot = nextspot(old, spot, spots);
+            }
+            return -1;
+        }
+
+        /* calcAdditionalChunks, Scatter.hpp:365-381: the (int) casts collapse to
+         * unsigned arithmetic and CUDA's ::max/::min(int, unsigned) compare unsigned. */
+        __device__ __forceinline__ u32 calc_additional_chunks(u32 pagesize, u32 fullsegments, u32 segmentsize,
+                                                              u32 chunksize)
+        {
+            if(fullsegments != 32u)
+                return umin(31u, (pagesize - fullsegments * segmentsize - 4u) / chunksize);
+            return 0u;
+        }
+
+        /* Capacity of a page formatted with chunksize (countFreeChunksInPage's
+         * capacity term, Scatter.hpp:1116-1138; tryUsePage's bound, :493-508). */
+        __device__ __forceinline__ u32 page_capacity(const mmc_device_handle& h, u32 chunksize)
+        {
+            if(chunksize <= h.hierarchyThreshold)
+            {
+                const u32 segmentsize = chunksize * 32u + 4u;
+                const u32 fullsegments = umin(32u, h.pagesize / segmentsize);
+                return fullsegments * 32u + calc_additional_chunks(h.pagesize, fullsegments, segmentsize, chunksize);
+            }
+            return umin(h.pagesize / chunksize, 32u);
+        }
+
+        /* addChunkHierarchy, Scatter.hpp:397-421 */
+        template<class Ids>
+        __device__ void* add_chunk_hierarchy(const mmc_device_handle& h, u32 chunksize, u32 fullsegments,
+                                             u32 additional_chunks, u32 page)
+        {
+            const u32 segments = fullsegments + (additional_chunks > 0u ? 1u : 0u);
+            u32 spot = Ids::laneid() % segments;
+            const u32 mask = ld_rlx(&h.bitmask[page]);
+            if((mask & (1u << spot)) != 0u)
+                spot = nextspot(mask, spot, segments);
+            const u32 tries = segments - static_cast<u32>(__popc(mask));
+            u32* onpagemasks = on_page_masks(h, page, segments);
+            for(u32 i = 0; i < tries; ++i)
+            {
+                const int hspot = usespot<Ids>(&onpagemasks[spot], spot < fullsegments ? 32u : additional_chunks);
+                if(hspot != -1)
+                    return page_data(h, page) + (32u * spot + static_cast<u32>(hspot)) * chunksize;
+                atomicOr(&h.bitmask[page], 1u << spot);
+                spot = nextspot(mask, spot, segments);
+            }
+            return nullptr;
+        }
+
+        /* addChunkNoHierarchy, Scatter.hpp:432-443 */
+        template<class Ids>
+        __device__ __forceinline__ void* add_chunk_no_hierarchy(const mmc_device_handle& h, u32 chunksize, u32 page,
+                                                                u32 spots)
+        {
+            const int spot = usespot<Ids>(&h.bitmask[page], spots);
+            if(spot == -1)
+                return nullptr;
+            return page_data(h, page) + static_cast<u32>(spot) * chunksize;
+        }
+
+        /* tryUsePage, Scatter.hpp:454-518; [lo, hi] is isChunkSizeInRange (:586-588). */
+        template<class Ids>
+        __device__ void* try_use_page(const mmc_device_handle& h, u32 page, u32 chunksize, u32 lo, u32 hi)
+        {
+            void* chunk_ptr = nullptr;
+            const u32 filllevel = atomicAdd(&h.count[page], 1u);
+            bool tryAllocMem = !h.resetfreedpages;
+            if(h.resetfreedpages && filllevel < h.pagesize)
+            {
+                const u32 oldChunksize = atomicCAS(&h.chunksize[page], 0u, chunksize);
+                if(oldChunksize == 0u || (oldChunksize >= lo && oldChunksize <= hi))
+                    tryAllocMem = true;
+                if(oldChunksize != 0u)
+                    chunksize = oldChunksize;
+            }
+            if(tryAllocMem)
+            {
+                if(chunksize <= h.hierarchyThreshold)
+                {
+                    const u32 segmentsize = chunksize * 32u + 4u;
+                    const u32 fullsegments = umin(32u, h.pagesize / segmentsize);
+                    const u32 additional_chunks
+                        = calc_additional_chunks(h.pagesize, fullsegments, segmentsize, chunksize);
+                    if(filllevel < fullsegments * 32u + additional_chunks)
+                        chunk_ptr = add_chunk_hierarchy<Ids>(h, chunksize, fullsegments, additional_chunks, page);
+                }
+                else
+                {
+                    const u32 chunksinpage = umin(h.pagesize / chunksize, 32u);
+                    if(filllevel < chunksinpage)
+                        chunk_ptr = add_chunk_no_hierarchy<Ids>(h, chunksize, page, chunksinpage);
+                }
+            }
+            if(chunk_ptr == nullptr)
+                atomicSub(&h.count[page], 1u);
+            return chunk_ptr;
+        }
+
+        /* allocChunked, Scatter.hpp:527-637 */
+        template<class Ids>
+        __device__ void* alloc_chunked(const mmc_device_handle& h, u32 bytes)
+        {
+            const u32 P = h.pagesize;
+            const u32 R = h.regionsize;
+            const u32 minAllocation = umax(bytes, h.paddedMinChunkSize);
+            const u32 numpages = h.numpages;
+            const u32 pagesperblock = h.pagesperblock;
+            const u32 reloff = Ids::warpSize * minAllocation / P;
+            const u32 start_page_in_block = (minAllocation * h.hashingK + h.hashingDistMP * Ids::smid()
+                                             + (h.hashingDistWP + h.hashingDistWPRel * reloff) * Ids::warpid())
+                % pagesperblock;
+            const u32 maxchunksize = umin(P, umax(h.wastefactor * bytes, h.paddedMinChunkSize));
+            u32 global_start_page = start_page_in_block + ld_rlx(&h.state->firstfreeblock) * pagesperblock;
+            if(global_start_page >= numpages)
+                global_start_page %= numpages; /* unreachable for a consistent header; keeps accesses in bounds */
+
+            u32 checklevel = R * 3u / 4u;
+            for(u32 finder = 0; finder < 2u; ++finder)
+            {
+                u32 global_page = global_start_page;
+                do
+                {
+                    const u32 region = global_page / R;
+                    const u32 regionfilllevel = ld_rlx(&h.regions[region]);
+                    const u32 region_offset = region * R;
+                    if(regionfilllevel < checklevel)
+                    {
+                        u32 page_in_region = global_page;
+                        do
+                        {
+                            const u32 beforeChunkSize = atomicCAS(&h.chunksize[page_in_region], 0u, minAllocation);
+                            u32 useChunkSize = 0u;
+                            if(beforeChunkSize == 0u)
+                                useChunkSize = minAllocation;
+                            else if(beforeChunkSize >= bytes && beforeChunkSize <= maxchunksize)
+                                useChunkSize = beforeChunkSize;
+                            if(useChunkSize != 0u)
+                            {
+                                void* res = try_use_page<Ids>(h, page_in_region, useChunkSize, bytes, maxchunksize);
+                                if(res != nullptr)
+                                    return res;
+                            }
+                            page_in_region = region_offset + ((page_in_region + 1u) % R);
+                        } while(page_in_region != global_page);
+
+                        if(regionfilllevel + 1u <= R)
+                            atomicCAS(&h.regions[region], regionfilllevel, regionfilllevel + 1u);
+                    }
+                    global_page = (global_page + R) % numpages;
+                    if(global_page % pagesperblock == 0u)
+                    {
+                        const u32 access_block_id = global_page / pagesperblock;
+                        /* racy by design (Scatter.hpp:625-628) */
+                        if(access_block_id > ld_rlx(&h.state->firstfreeblock))
+                            st_rlx(&h.state->firstfreeblock, access_block_id);
+                    }
+                } while(global_page != global_start_page);
+                checklevel = R + 1u;
+            }
+            return nullptr;
+        }
+
+        /* deallocChunked, Scatter.hpp:646-736 */
+        template<class Ids>
+        __device__ void dealloc_chunked(const mmc_device_handle& h, void* mem, u32 page, u32 chunksize)
+        {
+            const u32 P = h.pagesize;
+            const u32 inpage_offset = static_cast<u32>(static_cast<char*>(mem) - page_data(h, page));
+            if(chunksize <= h.hierarchyThreshold)
+            {
+                const u32 segmentsize = chunksize * 32u + 4u;
+                const u32 fullsegments = umin(32u, P / segmentsize);
+                const u32 additional_chunks = calc_additional_chunks(P, fullsegments, segmentsize, chunksize);
+                const u32 segment = inpage_offset / (chunksize * 32u);
+                const u32 withinsegment = (inpage_offset - segment * (chunksize * 32u)) / chunksize;
+                const u32 nMasks = fullsegments + (additional_chunks > 0u ? 1u : 0u);
+                u32* onpagemasks = on_page_masks(h, page, nMasks);
+                atomicAnd(&onpagemasks[segment], ~(1u << withinsegment));
+                atomicAnd(&h.bitmask[page], ~(1u << segment));
+            }
+            else
+            {
+                const u32 segment = inpage_offset / chunksize;
+                atomicAnd(&h.bitmask[page], ~(1u << segment));
+            }
+
+            u32 oldfilllevel = 0u;
+            if(h.resetfreedpages)
+            {
+                oldfilllevel = atomicCAS(&h.count[page], 1u, P);
+                if(oldfilllevel == 1u)
+                {
+                    page_init(h, page);
+                    atomicCAS(&h.chunksize[page], chunksize, 0u);
+                    __threadfence();
+                    atomicSub(&h.count[page], P);
+                }
+                else
+                    oldfilllevel = atomicSub(&h.count[page], 1u);
+            }
+            else
+                oldfilllevel = atomicSub(&h.count[page], 1u);
+
+            if(oldfilllevel == P / 2u / chunksize)
+            {
+                const u32 region = page / h.regionsize;
+                atomicExch(&h.regions[region], 0u);
+                const u32 block = page / h.pagesperblock;
+                if(Ids::warpid() + Ids::laneid() == 0u)
+                    atomicMin(&h.state->firstfreeblock, block);
+            }
+        }
+
+        /* chunk size seen by the page-based scan; index numpages (one past the end,
+         * which the reference's second search reads) counts as "in use". */
+        __device__ __forceinline__ u32 scan_chunksize(const mmc_device_handle& h, u32 page)
+        {
+            return page < h.numpages ? ld_rlx(&h.chunksize[page]) : 1u;
+        }
+
+        /* markpages, Scatter.hpp:745-764 */
+        __device__ inline bool markpages(const mmc_device_handle& h, u32 startpage, u32 pages, u32 bytes)
+        {
+            u32 abord = 0xFFFFFFFFu;
+            for(u32 trypage = startpage; trypage < startpage + pages; ++trypage)
+            {
+                const u32 old = atomicCAS(&h.chunksize[trypage], 0u, bytes);
+                if(old != 0u)
+                {
+                    abord = trypage;
+                    break;
+                }
+            }
+            if(abord == 0xFFFFFFFFu)
+                return true;
+            for(u32 trypage = startpage; trypage < abord; ++trypage)
+                atomicCAS(&h.chunksize[trypage], bytes, 0u);
+            return false;
+        }
+
+        /* allocPageBasedSingleRegion, Scatter.hpp:775-813 */
+        __device__ inline void* alloc_page_based_single_region(const mmc_device_handle& h, u32 startpage, u32 endpage,
+                                                        u32 bytes)
+        {
+            const u32 pagestoalloc = divup(bytes, h.pagesize);
+            u32 freecount = 0;
+            bool left_free = false;
+            for(u32 search_page = startpage + 1u; search_page > endpage;)
+            {
+                --search_page;
+                if(scan_chunksize(h, search_page) == 0u)
+                {
+                    if(++freecount == pagestoalloc)
+                    {
+                        if(search_page + pagestoalloc <= h.numpages && markpages(h, search_page, pagestoalloc, bytes))
+                        {
+                            if(!left_free)
+                            {
+                                /* the reference stores search_page - 1, which wraps for a
+                                 * run ending at page 0 (Scatter.hpp:800-804) */
+                                u32 nf = search_page - 1u;
+                                if(!h.reference_quirks && search_page == 0u)
+                                    nf = 0u;
+                                atomicCAS(&h.state->firstFreePageBased, startpage, nf);
+                            }
+                            return page_data(h, search_page);
+                        }
+                    }
+                }
+                else
+                {
+                    left_free = true;
+                    freecount = 0;
+                }
+            }
+            return nullptr;
+        }
+
+        /* allocPageBasedSingle, Scatter.hpp:824-840, with a bounded, backed-off mutex wait. */
+        __device__ inline void* alloc_page_based_single(const mmc_device_handle& h, u32 bytes)
+        {
+            u32 ns = 32u;
+            for(u32 it = 0; atomicExch(&h.state->pagebasedMutex, 1u) != 0u; ++it)
+            {
+                if(it >= MMC_MUTEX_MAX_SPINS)
+                {
+                    set_error(h, MMC_DEVERR_TIMEOUT);
+                    return nullptr;
+                }
+                __nanosleep(ns);
+                if(ns < 2048u)
+                    ns <<= 1;
+            }
+            __threadfence();
+            const u32 spage = ld_rlx(&h.state->firstFreePageBased);
+            void* res = alloc_page_based_single_region(h, spage, 0u, bytes);
+            if(res == nullptr)
+                res = alloc_page_based_single_region(h, h.numpages, spage, bytes);
+            __threadfence();
+            atomicExch(&h.state->pagebasedMutex, 0u);
+            return res;
+        }
+
+        /* allocPageBased, Scatter.hpp:848-866: the active lanes of a warp take turns. */
+        template<class Ids>
+        __device__ void* alloc_page_based(const mmc_device_handle& h, u32 bytes)
+        {
+            if(Ids::warpSize == 1u)
+                return alloc_page_based_single(h, bytes);
+            void* res = nullptr;
+            const u32 mask = __activemask();
+            const u32 num = static_cast<u32>(__popc(mask));
+            const u32 local_id = static_cast<u32>(__popc(lanemask_lt() & mask));
+            for(u32 active = 0; active < num; ++active)
+                if(active == local_id)
+                    res = alloc_page_based_single(h, bytes);
+            return res;
+        }
+
+        /* deallocPageBased, Scatter.hpp:874-886 */
+        __device__ inline void dealloc_page_based(const mmc_device_handle& h, u32 page, u32 bytes)
+        {
+            const u32 pages = divup(bytes, h.pagesize);
+            const u32 end = umin(page + pages, h.numpages);
+            for(u32 p = page; p < end; ++p)
+                page_init(h, p);
+            __threadfence();
+            for(u32 p = page; p < end; ++p)
+                atomicCAS(&h.chunksize[p], bytes, 0u);
+            atomicMax(&h.state->firstFreePageBased, page + pages - 1u);
+        }
+
+        /* create, Scatter.hpp:895-912 */
+        template<class Ids>
+        __device__ __forceinline__ void* create(const mmc_device_handle& h, u32 bytes)
+        {
+            if(bytes == 0u)
+                return nullptr;
+            if(bytes <= h.pagesize)
+                return alloc_chunked<Ids>(h, bytes);
+            return alloc_page_based<Ids>(h, bytes);
+        }
+
+        /* destroy, Scatter.hpp:918-946. A pointer outside the pool or on a page
+         * without a chunk size (where the reference would divide by zero) is
+         * recorded as MMC_DEVERR_BADFREE and ignored. */
+        template<class Ids>
+        __device__ void destroy(const mmc_device_handle& h, void* mem)
+        {
+            if(mem == nullptr)
+                return;
+            const u32 P = h.pagesize;
+            const u64 offset = static_cast<u64>(static_cast<char*>(mem) - h.pages);
+            if(offset >= static_cast<u64>(h.numpages) * P)
+            {
+                set_error(h, MMC_DEVERR_BADFREE);
+                return;
+            }
+            const u32 page = (P & (P - 1u)) == 0u ? static_cast<u32>(offset >> (__ffs(static_cast<int>(P)) - 1))
+                                                  : static_cast<u32>(offset / P);
+            const u32 chunksize = ld_rlx(&h.chunksize[page]);
+            if(chunksize == 0u)
+            {
+                set_error(h, MMC_DEVERR_BADFREE);
+                return;
+            }
+            const u32 inpage_offset = static_cast<u32>(offset - static_cast<u64>(page) * P);
+            const u32 block = inpage_offset / chunksize;
+            const u32 inblockoffset = inpage_offset - block * chunksize;
+            if(inblockoffset != 0u)
+            {
+                /* XMallocSIMD sub-allocation: the lane count lives at the chunk head */
+                u32* counter = reinterpret_cast<u32*>(page_data(h, page) + block * chunksize);
+                const u32 old = atomicSub(counter, 1u);
+                if(old != 1u)
+                    return;
+                mem = counter;
+            }
+            if(chunksize < P || (!h.reference_quirks && chunksize == P))
+                dealloc_chunked<Ids>(h, mem, page, chunksize);
+            else
+                dealloc_page_based(h, page, chunksize);
+        }
+
+        /* OOM policy: ReturnNull::handleOOM (ReturnNull.hpp:48-51); MMC_OOM_FLAG
+         * records the failure instead of BadAllocException's device assert. */
+        __device__ __forceinline__ void* handle_oom(const mmc_device_handle& h, void* mem, u32 req)
+        {
+            if(req != 0u && mem == nullptr && h.oom_policy == MMC_OOM_FLAG)
+                set_error(h, MMC_DEVERR_OOM);
+            return (req != 0u && mem == nullptr) ? nullptr : mem;
+        }
+
+        /* DeviceAllocator::malloc (device_allocator.hpp:72-82) with XMallocSIMD's
+         * collect/distribute (XMallocSIMD.hpp:118-176): every active lane whose
+         * padded size is in (0, pagesize/32) joins one allocation of
+         * 16 + sum(sizes); the lowest such lane requests it, writes the lane
+         * count at its head (the refcount destroy() decrements, Scatter.hpp:931-940)
+         * and each lane receives base + 16 + (sizes of lower lanes). */
+        template<class Ids>
+        __device__ void* malloc(const mmc_device_handle& h, size_t bytes_in)
+        {
+            const u32 bytes = apply_padding(h.dataAlignment, static_cast<u32>(bytes_in));
+            if(!Ids::coalesce || h.distribution != MMC_DIST_XMALLOCSIMD)
+            {
+                void* p = create<Ids>(h, bytes);
+                return handle_oom(h, p, bytes);
+            }
+            const u32 active = __activemask();
+            const bool coalescible = bytes > 0u && bytes < (h.pagesize / 32u);
+            const u32 cmask = __ballot_sync(active, coalescible);
+            const u32 threadcount = static_cast<u32>(__popc(cmask));
+            if(threadcount <= 1u)
+            {
+                void* p = create<Ids>(h, bytes);
+                return handle_oom(h, p, bytes);
+            }
+            /* exclusive prefix of the coalescible lanes' sizes, in lane order */
+            const u32 lane = Ids::laneid();
+            const u32 mine = coalescible ? bytes : 0u;
+            u32 before = 0u;
+            if(active == 0xFFFFFFFFu)
+            {
+                u32 incl = mine;
+#pragma unroll
+                for(u32 off = 1u; off < 32u; off <<= 1)
+                {
+                    const u32 v = __shfl_up_sync(0xFFFFFFFFu, incl, off);
+                    if(lane >= off)
+                        incl += v;
+                }
+                before = incl - mine;
+            }
+            else
+            {
+                for(u32 m = cmask; m != 0u; m &= m - 1u)
+                {
+                    const u32 src = static_cast<u32>(__ffs(static_cast<int>(m))) - 1u;
+                    const u32 v = __shfl_sync(active, mine, static_cast<int>(src));
+                    if(src < lane)
+                        before += v;
+                }
+            }
+            const u32 total = __reduce_add_sync(active, mine);
+            const u32 leader = static_cast<u32>(__ffs(static_cast<int>(cmask))) - 1u;
+            u32 req = bytes;
+            if(coalescible)
+                req = (lane == leader) ? 16u + total : 0u;
+            void* mem = create<Ids>(h, req);
+            mem = handle_oom(h, mem, req);
+            if(coalescible && lane == leader && mem != nullptr)
+                *static_cast<u32*>(mem) = threadcount;
+            const unsigned long long base
+                = __shfl_sync(active, reinterpret_cast<unsigned long long>(mem), static_cast<int>(leader));
+            if(!coalescible)
+                return mem;
+            return base != 0ull ? reinterpret_cast<char*>(base) + 16u + before : nullptr;
+        }
+
+        template<class Ids>
+        __device__ __forceinline__ void free(const mmc_device_handle& h, void* p)
+        {
+            destroy<Ids>(h, p);
+        }
+
+        /* ------------------------------------------------ free-slot counting */
+
+        /* Run summary of a page range for the multi-page slot count: the
+         * reference's serial scan (Scatter.hpp:1196-1217) counts
+         * floor(L / pagestoalloc) per maximal run of L free pages; runs are
+         * combined associatively so ranges can be scanned in parallel. */
+        struct RunSum
+        {
+            u32 len; /* pages covered */
+            u32 pre; /* free pages at the low end (== len if all free) */
+            u32 suf; /* free pages at the high end */
+            u32 cnt; /* slots in runs touching neither end */
+        };
+
+        __host__ __device__ __forceinline__ RunSum run_leaf(bool free_page)
+        {
+            return RunSum{1u, free_page ? 1u : 0u, free_page ? 1u : 0u, 0u};
+        }
+        __host__ __device__ __forceinline__ RunSum run_empty() { return RunSum{0u, 0u, 0u, 0u}; }
+
+        /* a covers lower page indices than b */
+        __host__ __device__ __forceinline__ RunSum run_combine(RunSum a, RunSum b, u32 n)
+        {
+            if(a.len == 0u)
+                return b;
+            if(b.len == 0u)
+                return a;
+            const bool af = a.pre == a.len;
+            const bool bf = b.pre == b.len;
+            RunSum r;
+            r.len = a.len + b.len;
+            if(af && bf)
+            {
+                r.pre = r.suf = r.len;
+                r.cnt = 0u;
+            }
+            else if(af)
+            {
+                r.pre = a.len + b.pre;
+                r.suf = b.suf;
+                r.cnt = b.cnt;
+            }
+            else if(bf)
+            {
+                r.pre = a.pre;
+                r.suf = a.suf + b.len;
+                r.cnt = a.cnt;
+            }
+            else
+            {
+                r.pre = a.pre;
+                r.suf = b.suf;
+                r.cnt = a.cnt + b.cnt + (a.suf + b.pre) / n;
+            }
+            return r;
+        }
+
+        __host__ __device__ __forceinline__ u32 run_total(RunSum s, u32 n)
+        {
+            if(s.len != 0u && s.pre == s.len)
+                return s.len / n;
+            return s.cnt + s.pre / n + s.suf / n;
+        }
+
+        __device__ __forceinline__ RunSum shfl_runsum(u32 mask, RunSum s, int src)
+        {
+            RunSum r;
+            r.len = __shfl_sync(mask, s.len, src);
+            r.pre = __shfl_sync(mask, s.pre, src);
+            r.suf = __shfl_sync(mask, s.suf, src);
+            r.cnt = __shfl_sync(mask, s.cnt, src);
+            return r;
+        }
+
+        /* Free slots of size slot on one page: getAvailaibleSlotsDeviceFunction's
+         * single-page branch (Scatter.hpp:1164-1193) with countFreeChunksInPage
+         * (:1112-1139). capZero = capacity at max(slot, paddedMinChunkSize). */
+        __device__ __forceinline__ u32 page_free_slots(const mmc_device_handle& h, u32 chunksize, u32 count,
+                                                       u32 slot, u32 maxchunksize, u32 slotChunk, u32 capSlotChunk)
+        {
+            if(chunksize >= slot && chunksize <= maxchunksize)
+                return (chunksize == slotChunk ? capSlotChunk : page_capacity(h, chunksize)) - count;
+            if(chunksize == 0u)
+                return capSlotChunk - count;
+            return 0u;
+        }
+
+        /* handle.getAvailableSlots (device_allocator.hpp:98-106 ->
+         * getAvailableSlotsAccelerator, Scatter.hpp:1311-1352): the lanes active
+         * at the call share the scan and all of them receive the count. Unlike
+         * the reference it needs no block-wide barrier, so any subset of threads
+         * may call it. slotSize is padded first (device_allocator.hpp:103). */
+        template<class Ids>
+        __device__ unsigned available_slots(const mmc_device_handle& h, size_t slotSize_in)
+        {
+            const u32 slot = apply_padding(h.dataAlignment, static_cast<u32>(slotSize_in));
+            if(slot == 0u)
+                return 0u;
+            u32 active = 1u, rank = 0u, nact = 1u;
+            if(Ids::warpSize > 1u)
+            {
+                active = __activemask();
+                nact = static_cast<u32>(__popc(active));
+                rank = static_cast<u32>(__popc(active & lanemask_lt()));
+            }
+            const u32 P = h.pagesize;
+            u32 partial = 0u;
+            if(slot < P)
+            {
+                const u32 maxchunksize = umin(P, h.wastefactor * slot);
+                const u32 slotChunk = umax(slot, h.paddedMinChunkSize);
+                const u32 capSlotChunk = page_capacity(h, slotChunk);
+                for(u32 pg = rank; pg < h.numpages; pg += nact)
+                    partial += page_free_slots(h, ld_rlx(&h.chunksize[pg]), ld_rlx(&h.count[pg]), slot, maxchunksize,
+                                               slotChunk, capSlotChunk);
+                if(Ids::warpSize > 1u)
+                    partial = __reduce_add_sync(active, partial);
+                return partial;
+            }
+            /* multi-page slots: each active lane summarises a contiguous range,
+             * the summaries are combined in lane order */
+            const u32 n = divup(slot, P);
+            const u32 per = divup(h.numpages, nact);
+            const u32 b = umin(rank * per, h.numpages);
+            const u32 e = umin(b + per, h.numpages);
+            RunSum s = run_empty();
+            for(u32 pg = b; pg < e; ++pg)
+                s = run_combine(s, run_leaf(ld_rlx(&h.chunksize[pg]) == 0u), n);
+            if(Ids::warpSize > 1u)
+            {
+                /* ordered fold over the active lanes, result broadcast */
+                RunSum acc = run_empty();
+                for(u32 m = active; m != 0u; m &= m - 1u)
+                {
+                    const int src = __ffs(static_cast<int>(m)) - 1;
+                    acc = run_combine(acc, shfl_runsum(active, s, src), n);
+                }
+                s = acc;
+            }
+            return run_total(s, n);
+        }
+    } // namespace dev
+} // namespace mmc

@@ -1,0 +1,250 @@
+/* mallocmc_gb300.h — C ABI of the GB300 (sm_103a) ScatterAlloc heap.
+ *
+ * A heap is a device-resident ScatterAlloc pool (pages, page-table entries,
+ * region fill counters) plus a small device header. Host code creates and
+ * queries it through these functions; kernels allocate from it through the
+ * device functions in <mallocMC/scatter_device.cuh> using the POD
+ * mmc_device_handle, passed to kernels by value.
+ *
+ * Each entry point names the reference interface it replaces (paths relative
+ * to the mallocMC project root). Conventions: every function returns an
+ * mmc_status (0 = success); mmc_last_error() gives a message for the calling
+ * thread's last failure. Host calls on one heap are stream-ordered and not
+ * thread-safe (the reference's queue semantics); device calls are fully
+ * concurrent. No exception crosses this boundary.
+ */
+#ifndef MALLOCMC_GB300_H
+#define MALLOCMC_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MMC_VERSION_MAJOR 2
+#define MMC_VERSION_MINOR 6
+#define MMC_VERSION_PATCH 0
+
+typedef enum mmc_status
+{
+    MMC_OK = 0,
+    MMC_ERR_CONFIG = 1,  /* invalid configuration (e.g. heap smaller than one access block) */
+    MMC_ERR_CUDA = 2,    /* a CUDA runtime call failed */
+    MMC_ERR_TIMEOUT = 3, /* a bounded device wait gave up (see mmc_heap_error) */
+    MMC_ERR_OOM = 4,     /* the pool could not be allocated */
+    MMC_ERR_ARG = 5      /* bad argument (null pointer, size out of range) */
+} mmc_status;
+
+/* Distribution policies (src/include/mallocMC/distributionPolicies/). */
+#define MMC_DIST_NOOP 0        /* DistributionPolicies::Noop (Noop.hpp:46-72) */
+#define MMC_DIST_XMALLOCSIMD 1 /* DistributionPolicies::XMallocSIMD (XMallocSIMD.hpp:76-185) */
+
+/* OOM policies (src/include/mallocMC/oOMPolicies/). */
+#define MMC_OOM_RETURNNULL 0 /* OOMPolicies::ReturnNull (ReturnNull.hpp:44-57) */
+#define MMC_OOM_FLAG 1       /* BadAllocException's device branch without the trap: sets MMC_DEVERR_OOM, returns NULL */
+
+/* Device error bits reported by mmc_heap_error. */
+#define MMC_DEVERR_TIMEOUT 0x1u  /* the page-based mutex wait hit its iteration bound */
+#define MMC_DEVERR_BADFREE 0x2u  /* free of a pointer outside the heap or on an unformatted page */
+#define MMC_DEVERR_OOM 0x4u      /* an allocation failed under MMC_OOM_FLAG */
+
+/* Heap configuration: the template parameters of Scatter<HeapConfig, HashConfig>
+ * (creationPolicies/Scatter.hpp:56-85, 124-207), XMallocSIMD<Config> and
+ * Shrink<Config> (alignmentPolicies/Shrink.hpp:62-65) as runtime values. */
+typedef struct mmc_config
+{
+    uint32_t pagesize;         /* bytes per page (>= 1024, multiple of 16) */
+    uint32_t regionsize;       /* pages per region */
+    uint32_t wastefactor;      /* chunk reuse bound: chunksize <= wastefactor * bytes */
+    uint32_t resetfreedpages;  /* 1: a fully freed page forgets its chunk size */
+    uint64_t accessblocksize;  /* bytes per access block (heap must hold at least one) */
+    uint32_t hashingK;         /* page-hash multiplier of the request size */
+    uint32_t hashingDistMP;    /* page-hash multiplier of the SM id */
+    uint32_t hashingDistWP;    /* page-hash multiplier of the warp id */
+    uint32_t hashingDistWPRel; /* page-hash multiplier of warp id x relative size */
+    uint32_t dataAlignment;    /* Shrink alignment (power of two); 0 or 1 = AlignmentPolicies::Noop */
+    uint32_t distribution;     /* MMC_DIST_* */
+    uint32_t oom_policy;       /* MMC_OOM_* */
+    uint32_t reference_quirks; /* 1: keep the reference's exact-pagesize free and page-based
+                                  underflow behaviour bit for bit (default); 0: fixed */
+} mmc_config;
+
+/* Fill *cfg with the reference defaults: DefaultScatterConfig/DefaultScatterHashingParams
+ * (Scatter.hpp:56-85), XMallocSIMD, ReturnNull, Shrink<16>. */
+void mmc_config_default(mmc_config* cfg);
+
+/* Device-resident mutable header words (one per heap, 128-byte separated). */
+typedef struct mmc_heap_state mmc_heap_state;
+
+/* Everything a kernel needs to allocate, passed by value (kernel parameter
+ * space). The reference's AllocatorHandleImpl holds a pointer to the device
+ * allocator object (mallocMC_allocator_handle.hpp:35-63); here the immutable
+ * fields travel with the handle and only the mutable words live in memory. */
+typedef struct mmc_device_handle
+{
+    mmc_heap_state* state;
+    char* pages;         /* page i starts at pages + i * pagesize (= pool start) */
+    uint32_t* chunksize; /* per-page chunk size (page-table entry word 0) */
+    uint32_t* count;     /* per-page fill count (word 1) */
+    uint32_t* bitmask;   /* per-page chunk / segment bitmask (word 2) */
+    uint32_t* regions;   /* per-region fill counters */
+    uint32_t numpages;
+    uint32_t numregions;
+    uint32_t accessblocks;
+    uint32_t pagesperblock;
+    uint32_t pagesize;
+    uint32_t regionsize;
+    uint32_t wastefactor;
+    uint32_t resetfreedpages;
+    uint32_t hashingK;
+    uint32_t hashingDistMP;
+    uint32_t hashingDistWP;
+    uint32_t hashingDistWPRel;
+    uint32_t dataAlignment;
+    uint32_t distribution;
+    uint32_t oom_policy;
+    uint32_t reference_quirks;
+    uint32_t hierarchyThreshold; /* (pagesize - 8) / 33 */
+    uint32_t minChunkSize;       /* (pagesize - 128) / 1024 */
+    uint32_t paddedMinChunkSize; /* minChunkSize after alignment padding */
+    uint32_t maxOnPageMasks;     /* min(32, ceil(pagesize / (32 * minChunkSize + 4))) */
+} mmc_device_handle;
+
+typedef struct mmc_heap mmc_heap;
+
+/* Heap geometry, as initDeviceFunction computes it (Scatter.hpp:956-1049). */
+typedef struct mmc_geometry
+{
+    uint64_t memsize;
+    uint32_t numpages;
+    uint32_t numregions;
+    uint32_t accessblocks;
+    uint32_t pagesperblock;
+    uint32_t maxOnPageMasks;
+    uint32_t hierarchyThreshold;
+    uint64_t ptes_offset;    /* byte offset of the page-table arrays from the pool start */
+    uint64_t regions_offset; /* byte offset of the region counters from the pool start */
+} mmc_geometry;
+
+/* ---------------------------------------------------------------- lifetime */
+
+/* Allocator::Allocator(dev, queue, size) / alloc (allocator.hpp:136-159, 179-183):
+ * cudaMalloc a pool of `bytes` on `device` (ReservePoolPolicies::AlpakaBuf,
+ * AlpakaBuf.hpp:41-46), align it (Shrink::alignPool, Shrink.hpp:109-130) and
+ * initialise the heap on `stream` (Scatter::initHeap, Scatter.hpp:1057-1096).
+ * MMC_ERR_CONFIG where the reference would divide by zero (heap smaller than
+ * one access block, Scatter.hpp:991-993). */
+mmc_status mmc_heap_create(const mmc_config* cfg, size_t bytes, int device, void* stream, mmc_heap** out);
+
+/* Like mmc_heap_create over a caller-owned device pool (not freed by the heap).
+ * Scatter::initHeap's nullptr check (Scatter.hpp:1065-1071) is MMC_ERR_ARG. */
+mmc_status mmc_heap_create_on_pool(const mmc_config* cfg, void* pool, size_t bytes, int device, void* stream,
+                                   mmc_heap** out);
+
+/* ~Allocator / free (allocator.hpp:166-172, 185-189). */
+mmc_status mmc_heap_destroy(mmc_heap* heap);
+
+/* Allocator::destructiveResize (allocator.hpp:195-200): drop every allocation,
+ * reallocate the pool with `bytes` and initialise it again. */
+mmc_status mmc_heap_destructive_resize(mmc_heap* heap, size_t bytes, void* stream);
+
+/* Allocator::getAllocatorHandle / operator AllocatorHandle (allocator.hpp:202-212). */
+mmc_status mmc_heap_device_handle(const mmc_heap* heap, mmc_device_handle* out);
+
+/* Allocator::getHeapLocations (allocator.hpp:235-241): the pool start and size. */
+mmc_status mmc_heap_locations(const mmc_heap* heap, void** pool, size_t* size);
+
+/* Geometry of the initialised heap (numpages etc., Scatter.hpp:962-1048). */
+mmc_status mmc_heap_geometry(const mmc_heap* heap, mmc_geometry* out);
+
+/* Allocator::info (allocator.hpp:214-223) joined with Scatter::classname
+ * (Scatter.hpp:1354-1370): writes a NUL-terminated description. */
+mmc_status mmc_heap_info(const mmc_heap* heap, char* buf, size_t len);
+
+/* ------------------------------------------------------------- free slots */
+
+/* Allocator::getAvailableSlots (allocator.hpp:227-233 -> Scatter::getAvailableSlotsHost,
+ * Scatter.hpp:1235-1295): pads slot_size, counts free slots of that size and
+ * waits for the result (*out, an unsigned that wraps like the reference's). */
+mmc_status mmc_available_slots(mmc_heap* heap, size_t slot_size, void* stream, unsigned* out);
+
+/* Stream-ordered variant with no host synchronisation: the count is written
+ * to *out_dev (device or mapped memory) when the stream reaches it. Safe to
+ * capture in a CUDA graph once the heap exists. */
+mmc_status mmc_available_slots_async(mmc_heap* heap, size_t slot_size, void* stream, unsigned* out_dev);
+
+/* --------------------------------------------------------- introspection */
+
+/* Device error bits (MMC_DEVERR_*) accumulated since the last clear; waits for
+ * `stream`. clear != 0 resets them. */
+mmc_status mmc_heap_error(mmc_heap* heap, void* stream, uint32_t* flags, int clear);
+
+/* Copy the metadata to host buffers (each may be NULL): ptes3 = numpages x
+ * {chunksize, count, bitmask}; regions = numregions words; masks = numpages x
+ * maxOnPageMasks words (the last words of each page); header3 =
+ * {firstFreePageBased, firstfreeblock, pagebasedMutex}. Waits for `stream`. */
+mmc_status mmc_snapshot_metadata(mmc_heap* heap, void* stream, uint32_t* ptes3, uint32_t* regions, uint32_t* masks,
+                                 uint32_t* header3);
+
+/* Message for the calling thread's last failed call ("" if none). */
+const char* mmc_last_error(void);
+
+/* ------------------------------------------------------------- workloads
+ * Kernels built on the device API (what user kernels do with handle.malloc /
+ * handle.free), exported for verification, benchmarking and batching. All
+ * pointers are device pointers unless stated; all run on `stream`. */
+
+/* Run an op program in ONE device thread with the reference CPU backend's
+ * thread ids (laneid = warpid = smid = 0, warp size 1, mallocMC_utils.hpp:72-136),
+ * so pool offsets are bit-identical to the reference's CPU-serial run.
+ * kinds[i]: 'm' malloc(args[i]) -> out[i] = pool offset or -1; 'f' free the
+ * block returned by op args[i] (an op index); 'd' handle.getAvailableSlots(args[i])
+ * -> out[i]; 's' Allocator::getAvailableSlots(args[i]) -> out[i]; other kinds
+ * are no-ops. kinds/args/out are device buffers of n entries. */
+mmc_status mmc_run_program(mmc_heap* heap, const uint8_t* kinds, const uint64_t* args, int64_t n, int64_t* out,
+                           void* stream);
+
+/* Uniform stress (every thread `rounds` x {malloc(size), write a u64 pattern,
+ * verify it, free}). Sizes: sizes[t * rounds + r] (u16, bytes) if sizes != NULL,
+ * else drawn from seed uniformly in {lo, lo+step, ..., hi}. stats (device, 4 x u64,
+ * accumulated, caller zeroes): {pairs, nulls, pattern errors, checksum}. */
+typedef struct mmc_stress_params
+{
+    uint32_t blocks;
+    uint32_t threads_per_block;
+    uint32_t rounds;
+    uint32_t lo, hi, step;
+    uint64_t seed;
+    uint32_t write_pattern; /* 0: allocate/free only */
+    uint32_t reserved;
+} mmc_stress_params;
+mmc_status mmc_run_stress(mmc_heap* heap, const mmc_stress_params* p, const uint16_t* sizes,
+                          unsigned long long* stats, void* stream);
+
+/* The plain ScatterAlloc verify workload: every thread mallocs sizes[t] bytes,
+ * writes the u32 pattern (t ^ seed), verifies it, frees. offsets[t] receives
+ * the pool offset (or -1), errors[0] the count of failed words (both device). */
+mmc_status mmc_run_verify(mmc_heap* heap, uint32_t blocks, uint32_t threads_per_block, const uint32_t* sizes,
+                          uint32_t seed, int64_t* offsets, unsigned long long* errors, void* stream);
+
+/* Split a verify run into its halves: every thread mallocs sizes[t] and writes
+ * its pattern (offsets[t] = pool offset or -1); then the caller inspects the
+ * heap; then mmc_run_free_offsets verifies and frees them. */
+mmc_status mmc_run_alloc_offsets(mmc_heap* heap, uint32_t blocks, uint32_t threads_per_block, const uint32_t* sizes,
+                                 uint32_t seed, int64_t* offsets, void* stream);
+mmc_status mmc_run_free_offsets(mmc_heap* heap, uint32_t blocks, uint32_t threads_per_block, const uint32_t* sizes,
+                                uint32_t seed, const int64_t* offsets, unsigned long long* errors, void* stream);
+
+/* Relaxed device-scope atomicOr throughput over `words` u32 words at `buf`
+ * (device, zeroed by the caller): iters per thread, random word per op.
+ * returning != 0 uses the value (atom), else it is discarded (red).
+ * contended != 0 makes every lane of a warp hit the same word. */
+mmc_status mmc_atomic_peak(uint32_t* buf, uint64_t words, uint32_t blocks, uint32_t threads_per_block, uint32_t iters,
+                           int returning, int contended, unsigned long long* sink, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MALLOCMC_GB300_H */

@@ -1,0 +1,32 @@
+/* Internal helpers shared by the translation units of libmallocmc_gb300.so. */
+#pragma once
+
+#include "mallocmc_gb300.h"
+#include "mallocMC/scatter_device.cuh"
+
+#include <cuda_runtime.h>
+
+#include <string>
+
+namespace mmc
+{
+    namespace host
+    {
+        /* Record msg as the calling thread's last error and return st. */
+        mmc_status fail(mmc_status st, const std::string& msg);
+        /* If e is an error: record it (with what) and return MMC_ERR_CUDA. */
+        mmc_status cuda_check(cudaError_t e, const char* what);
+
+        inline cudaStream_t as_stream(void* s) { return static_cast<cudaStream_t>(s); }
+
+        /* Grid for whole-heap scans: a multiple of the SM count. */
+        unsigned scan_grid(int device);
+
+        /* Launch the two-pass free-slot count of `slot` (already padded) and
+         * leave the unsigned result in *result_dev (device memory). */
+        mmc_status launch_available_slots(mmc_heap* heap, uint32_t slot, cudaStream_t s, unsigned* result_dev);
+
+        /* Device-side word that receives the result of mmc_available_slots. */
+        unsigned* slots_result_word(mmc_heap* heap);
+    } // namespace host
+} // namespace mmc

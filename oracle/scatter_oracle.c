@@ -699,8 +699,6 @@ void oc_load_state(oc_heap* h, const uint32_t* ptes3, const uint32_t* regions, c
 
 void oc_run_program(oc_heap* h, const uint8_t* kinds, const uint64_t* args, int64_t n, int64_t* out)
 {
-    void** ptrs = (void**) calloc((size_t) (n > 0 ? n : 1), sizeof(void*));
-    int64_t nm = 0;
     for(int64_t i = 0; i < n; ++i)
     {
         out[i] = 0;
@@ -709,20 +707,21 @@ void oc_run_program(oc_heap* h, const uint8_t* kinds, const uint64_t* args, int6
         case 'm':
         {
             void* p = oc_malloc(h, args[i]);
-            ptrs[nm++] = p;
             out[i] = p ? (int64_t) ((uint8_t*) p - h->pool) : -1;
             break;
         }
         case 'f':
-            if((int64_t) args[i] < nm)
-                oc_free(h, ptrs[args[i]]);
+        {
+            const int64_t j = (int64_t) args[i];
+            if(j >= 0 && j < i && kinds[j] == 'm' && out[j] >= 0)
+                oc_free(h, h->pool + out[j]);
             break;
+        }
         case 's': out[i] = oc_available_slots(h, args[i]); break;
         case 'd': out[i] = oc_available_slots_accelerator(h, args[i]); break;
         default: break;
         }
     }
-    free(ptrs);
 }
 
 uint64_t oc_mix64(uint64_t seed, uint64_t a, uint64_t b)

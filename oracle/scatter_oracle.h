@@ -85,8 +85,9 @@ void oc_snapshot_masks(oc_heap* h, uint32_t* out);
 void oc_load_state(oc_heap* h, const uint32_t* ptes3, const uint32_t* regions, const uint32_t* masks);
 
 /* Run an op program in one thread: ops[i] = {kind, arg}; kind 'm' malloc(arg),
- * 'f' free(result of the arg-th malloc), 's' host slots(arg), 'd' accelerator
- * slots(arg). out[i] = pool offset (malloc; -1 for null), slot count, or 0. */
+ * 'f' free the block returned by op number arg, 's' host slots(arg), 'd'
+ * accelerator slots(arg). out[i] = pool offset (malloc; -1 for null), slot
+ * count, or 0 (the same program format as the C ABI's mmc_run_program). */
 void oc_run_program(oc_heap* h, const uint8_t* kinds, const uint64_t* args, int64_t n, int64_t* out);
 
 /* Seeded request sizes shared with the CUDA workloads (SplitMix64 finaliser of

@@ -107,8 +107,13 @@ def fill_program(cfg, heap_bytes, seed, name):
     perm = rng.permutation(len(live))[: len(live) // 2]
     frees = [("f", live[int(i)]) for i in sorted(perm)]
     phase2 = [("m", draw()) for _ in range(n1 // 2 + 64)]
-    return phase1 + [("s", 16), ("s", 4 * P), ("S", 0)] + frees + [("s", 16)] + phase2 + [("s", 16), ("s", 4 * P),
-                                                                                        ("S", 0)]
+    head = phase1 + [("s", 16), ("s", 4 * P), ("S", 0)] + frees + [("s", 16)]
+    # keep phase 2 up to 40 mallocs past its first null: every failing malloc
+    # walks the whole heap, which is slow to replay in one device thread
+    res = run_reference(name, heap_bytes, program_text(head + phase2))
+    offs2 = [r[2] for r in res["results"][len(head):] if r[0] == "m"]
+    cut = (offs2.index(-1) + 41) if -1 in offs2 else len(offs2)
+    return head + phase2[:cut] + [("s", 16), ("s", 4 * P), ("S", 0)]
 
 
 def make_case(name, cfg_name, heap_bytes, ops):

@@ -1,0 +1,168 @@
+"""verify_heap-style checks of concurrent GPU runs (reference: tests/verify_heap.cpp).
+
+Concurrent placements depend on %smid/%warpid, so parity here is by
+properties: every returned block lies inside the page area, honours the
+alignment, overlaps no other live block, holds its per-thread pattern intact;
+freeing everything returns the page-table counts and bitmasks and the on-page
+masks to zero exactly; getAvailableSlots equals the oracle's count on the same
+heap state (and, with resetfreedpages, its pre-run value).
+"""
+import numpy as np
+import pytest
+
+from oracle.oracle import HeapConfig, OracleHeap, mix64
+from tests.test_parity_gpu import gpu_allocator
+
+pytestmark = pytest.mark.gpu
+
+
+def check_live_blocks(offs, sizes, numpages, pagesize, align=16):
+    ok = offs >= 0
+    o = offs[ok]
+    s = ((sizes[ok].astype(np.int64) + align - 1) // align) * align
+    assert np.all(o % align == 0), "misaligned block"
+    assert np.all(o + s <= numpages * pagesize), "block outside the page area"
+    order = np.argsort(o, kind="stable")
+    o, s = o[order], s[order]
+    assert np.all(o[:-1] + s[:-1] <= o[1:]), "overlapping live blocks"
+    return int(ok.sum())
+
+
+def assert_all_free(snap):
+    ptes, regions, masks, hdr = snap
+    assert int(ptes[:, 1].max(initial=0)) == 0, "page fill counts not back to zero"
+    assert int(ptes[:, 2].max(initial=0)) == 0, "page bitmasks not back to zero"
+    assert int(masks.max(initial=0)) == 0, "on-page masks not back to zero"
+    assert hdr["pagebasedMutex"] == 0
+
+
+@pytest.mark.parametrize("reset", [False, True])
+def test_verify_workload_4x256(reset):
+    """The plain verify run: 64 MiB, pagesize 4096, access block 8 MiB, XMallocSIMD,
+    ReturnNull, Shrink<16>; 4 blocks x 256 threads; sizes from {16,32,64,128}."""
+    from mallocmc_gb300.workloads import alloc_offsets, free_offsets
+
+    cfg = HeapConfig(4096, 8 << 20, 16, 2, reset)
+    seed = 12345
+    n = 4 * 256
+    sizes = (16 << (mix64(seed, np.arange(n), 0) % np.uint64(4)).astype(np.int64)).astype(np.uint32)
+    with gpu_allocator(cfg, 64 << 20) as alloc:
+        g = alloc.geometry()
+        before = alloc.getAvailableSlots(16)
+        ds, offs_t = alloc_offsets(alloc, 4, 256, sizes, seed)
+        offs = offs_t.cpu().numpy()
+        assert np.all(offs >= 0)
+        check_live_blocks(offs, sizes, g.numpages, 4096)
+        errors = free_offsets(alloc, 4, 256, ds, offs_t, seed)
+        assert errors == 0
+        snap = alloc.snapshot()
+        assert_all_free(snap)
+        after = alloc.getAvailableSlots(16)
+        assert alloc.error_flags() == 0
+    if reset:
+        assert after == before
+    else:
+        oh = OracleHeap(cfg, 64 << 20)
+        oh.load_state(snap[0], snap[1], snap[2])
+        assert after == oh.available_slots(16)
+
+
+def test_single_kernel_verify_and_damage_negative():
+    """mmc_run_verify in one kernel, then the reference's negative test
+    (verify_heap.cpp:399-405, 676-688): a corrupted word must be detected."""
+    import torch
+
+    from mallocmc_gb300.workloads import alloc_offsets, free_offsets, run_verify
+
+    cfg = HeapConfig(4096, 8 << 20, 16, 2, False)
+    n = 64 * 128
+    rng = np.random.default_rng(3)
+    sizes = (16 * rng.integers(1, 65, size=n)).astype(np.uint32)
+    with gpu_allocator(cfg, 256 << 20) as alloc:
+        offs, errors = run_verify(alloc, 64, 128, sizes, 99)
+        assert errors == 0 and np.all(offs >= 0)
+        ds, offs_t = alloc_offsets(alloc, 64, 128, sizes, 99)
+        pool = alloc.getHeapLocations()[0].p
+        victim = int(offs_t[1].item())
+
+        class _Word:  # one u32 of the second block, seen through the CUDA array interface
+            __cuda_array_interface__ = {"shape": (1,), "typestr": "<u4", "data": (pool + victim, False),
+                                        "version": 3}
+
+        torch.as_tensor(_Word(), device="cuda").fill_(5 * 750 - 1)
+        torch.cuda.synchronize()
+        assert free_offsets(alloc, 64, 128, ds, offs_t, 99) == 1
+        assert_all_free(alloc.snapshot())
+
+
+def test_stress_full_grid_small_heap():
+    """Many rounds of malloc/write/verify/free from a full GPU grid."""
+    import torch
+
+    from mallocmc_gb300.workloads import run_stress
+
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    cfg = HeapConfig(4096, 64 << 20, 16, 2, False)
+    with gpu_allocator(cfg, 1 << 30) as alloc:
+        st = run_stress(alloc, sms * 4, 256, 20, 16, 1024, 16, seed=1)
+        assert st["pairs"] == sms * 4 * 256 * 20
+        assert st["nulls"] == 0 and st["bad"] == 0
+        assert_all_free(alloc.snapshot())
+        assert alloc.error_flags() == 0
+
+
+def test_xmallocsimd_coalesces_in_lane_order():
+    """All 32 lanes request 16 B: one chunk of 16 + 32*16 bytes per warp, the
+    lane count at its head, lane k at base + 16 + 16k (XMallocSIMD.hpp:118-176)."""
+    from mallocmc_gb300.workloads import alloc_offsets, free_offsets
+
+    cfg = HeapConfig(4096, 8 << 20, 16, 2, False)
+    n = 8 * 128
+    sizes = np.full(n, 16, dtype=np.uint32)
+    with gpu_allocator(cfg, 64 << 20) as alloc:
+        ds, offs_t = alloc_offsets(alloc, 8, 128, sizes, 1)
+        offs = offs_t.cpu().numpy().reshape(-1, 32)
+        base = offs[:, :1] - 16
+        assert np.array_equal(offs - base, np.tile(16 + 16 * np.arange(32), (offs.shape[0], 1)))
+        ptes = alloc.snapshot()[0]
+        # each warp's chunk is one fill slot of a page formatted for 16 + 512 bytes
+        assert int(ptes[:, 1].sum()) == offs.shape[0]
+        assert set(np.unique(ptes[ptes[:, 1] > 0, 0])) <= {528, 544}
+        assert free_offsets(alloc, 8, 128, ds, offs_t, 1) == 0
+        assert_all_free(alloc.snapshot())
+
+
+def test_noop_distribution_does_not_coalesce():
+    from mallocmc_gb300.workloads import alloc_offsets, free_offsets
+
+    cfg = HeapConfig(4096, 8 << 20, 16, 2, False, xmallocsimd=False)
+    n = 4 * 128
+    sizes = np.full(n, 16, dtype=np.uint32)
+    with gpu_allocator(cfg, 64 << 20) as alloc:
+        ds, offs_t = alloc_offsets(alloc, 4, 128, sizes, 1)
+        offs = offs_t.cpu().numpy()
+        check_live_blocks(offs, sizes, alloc.geometry().numpages, 4096)
+        assert int(alloc.snapshot()[0][:, 1].sum()) == n
+        assert free_offsets(alloc, 4, 128, ds, offs_t, 1) == 0
+        assert_all_free(alloc.snapshot())
+
+
+def test_page_based_allocations_concurrent():
+    """Multi-page requests from many threads (global mutex path, Scatter.hpp:824-866)."""
+    from mallocmc_gb300.workloads import alloc_offsets, free_offsets
+
+    cfg = HeapConfig(4096, 16 << 20, 16, 2, False)
+    n = 8 * 64
+    rng = np.random.default_rng(8)
+    sizes = (16 * rng.integers(260, 1400, size=n)).astype(np.uint32)  # 4 KiB .. 22 KiB
+    with gpu_allocator(cfg, 128 << 20) as alloc:
+        g = alloc.geometry()
+        ds, offs_t = alloc_offsets(alloc, 8, 64, sizes, 4)
+        offs = offs_t.cpu().numpy()
+        assert np.all(offs >= 0)
+        check_live_blocks(offs, sizes, g.numpages, 4096)
+        assert free_offsets(alloc, 8, 64, ds, offs_t, 4) == 0
+        ptes, regions, masks, hdr = alloc.snapshot()
+        assert int(ptes[:, 0].max()) <= 4096  # every multi-page run released
+        assert_all_free((ptes, regions, masks, hdr))
+        assert alloc.error_flags() == 0
