@@ -213,10 +213,17 @@ namespace mmc
             u32* onpagemasks = on_page_masks(h, page, segments);
             for(u32 i = 0; i < tries; ++i)
             {
-                const int hspot = usespot<Ids>(&onpagemasks[spot], spot < fullsegments ? 32u : additional_chunks);
+                const u32 spots = spot < fullsegments ? 32u : additional_chunks;
+                const int hspot = usespot<Ids>(&onpagemasks[spot], spots);
                 if(hspot != -1)
                     return page_data(h, page) + (32u * spot + static_cast<u32>(hspot)) * chunksize;
                 atomicOr(&h.bitmask[page], 1u << spot);
+                /* A free in this segment may have cleared the hint just before
+                 * it was set; undo a mark the segment no longer deserves so no
+                 * stale "full" bit outlives the chunks. A lone thread only gets
+                 * here for a full segment, so this never fires serially. */
+                if(static_cast<u32>(__popc(ld_rlx(&onpagemasks[spot]))) < spots)
+                    atomicAnd(&h.bitmask[page], ~(1u << spot));
                 spot = nextspot(mask, spot, segments);
             }
             return nullptr;
@@ -363,15 +370,28 @@ namespace mmc
             if(h.resetfreedpages)
             {
                 oldfilllevel = atomicCAS(&h.count[page], 1u, P);
-                if(oldfilllevel == 1u)
+                bool locked = oldfilllevel == 1u;
+                if(!locked)
+                {
+                    oldfilllevel = atomicSub(&h.count[page], 1u);
+                    /* The reference resets a page only when a freer's CAS sees
+                     * count == 1, so two last frees racing past each other leave
+                     * it formatted. A freer that took the count from 1 to 0 takes
+                     * the same lock (count = pagesize) if nobody has claimed the
+                     * page since; a lone thread never gets here with old == 1. */
+                    if(oldfilllevel == 1u)
+                        locked = atomicCAS(&h.count[page], 0u, P) == 0u;
+                }
+                if(locked)
                 {
                     page_init(h, page);
+                    /* no chunk is live under the lock: drop any segment hint a
+                     * race left behind (a no-op for the reference's serial runs) */
+                    atomicExch(&h.bitmask[page], 0u);
                     atomicCAS(&h.chunksize[page], chunksize, 0u);
                     __threadfence();
                     atomicSub(&h.count[page], P);
                 }
-                else
-                    oldfilllevel = atomicSub(&h.count[page], 1u);
             }
             else
                 oldfilllevel = atomicSub(&h.count[page], 1u);

@@ -20,8 +20,10 @@ INCLUDE = os.path.join(ROOT, "include")
 BUILD_DIR = os.path.join(PKG, "_build")
 LIB_NAME = "libmallocmc_gb300.so"
 LIB_PATH = os.path.join(PKG, LIB_NAME)
+EXAMPLES_PATH = os.path.join(PKG, "libmallocmc_examples.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["heap_capi.cu", "workloads.cu"]
+EXAMPLE_SOURCES = ["cxx_examples.cu"]  # user-side code on the C++ API, linked against the library
 
 
 def nvcc() -> str:
@@ -55,6 +57,13 @@ def build(verbose: bool = False, ptxas_verbose: bool = False) -> str:
     os.makedirs(BUILD_DIR, exist_ok=True)
     hdrs = _headers()
     objs, jobs = [], []
+    ex_objs = []
+    for src in EXAMPLE_SOURCES:
+        s = os.path.join(CSRC, src)
+        o = os.path.join(BUILD_DIR, src.replace(".cu", ".o"))
+        ex_objs.append(o)
+        if _stale(o, [s] + hdrs):
+            jobs.append([nvcc()] + _flags() + ["-c", s, "-o", o])
     for src in SOURCES:
         s = os.path.join(CSRC, src)
         o = os.path.join(BUILD_DIR, src.replace(".cu", ".o"))
@@ -75,6 +84,12 @@ def build(verbose: bool = False, ptxas_verbose: bool = False) -> str:
                 raise RuntimeError(f"nvcc failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
     if _stale(LIB_PATH, objs):
         cmd = [nvcc()] + ARCH + ["-shared", "-cudart", "static", "-o", LIB_PATH] + objs
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    if _stale(EXAMPLES_PATH, ex_objs + [LIB_PATH]):
+        cmd = [nvcc()] + ARCH + ["-shared", "-cudart", "static", "-o", EXAMPLES_PATH] + ex_objs + \
+            ["-L" + PKG, "-lmallocmc_gb300", "-Xlinker", "-rpath,$ORIGIN"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")

@@ -1,0 +1,64 @@
+"""The C++ drop-in API (include/mallocMC/mallocMC.hpp) used the way the
+reference's examples use mallocMC (examples/mallocMC_example01.cpp,
+examples/mallocMC_example03.cpp), via libmallocmc_examples.so."""
+import ctypes
+import os
+
+import numpy as np
+import pytest
+
+from oracle.oracle import HeapConfig, OracleHeap
+
+
+@pytest.fixture(scope="module")
+def ex():
+    from mallocmc_gb300 import build
+
+    if not os.path.exists(build.EXAMPLES_PATH):
+        build.build()
+    L = ctypes.CDLL(build.EXAMPLES_PATH)
+    L.mmcx_example01.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_ulonglong),
+                                 ctypes.POINTER(ctypes.c_ulonglong), ctypes.POINTER(ctypes.c_uint),
+                                 ctypes.POINTER(ctypes.c_int)]
+    L.mmcx_example03.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint)]
+    L.mmcx_bad_config.argtypes = [ctypes.c_int]
+    L.mmcx_info.argtypes = [ctypes.c_char_p, ctypes.c_size_t]
+    return L
+
+
+def test_info_strings(ex):
+    buf = ctypes.create_string_buffer(4096)
+    assert ex.mmcx_info(buf, len(buf)) == 0
+    s = buf.value.decode()
+    assert "CreationPolicy:      Scatter[pagesize=4096,accessblocksize=268435456,regionsize=16" in s
+    assert "HierarchyThreshold=123" in s and "minChunkSize=3" in s
+    assert "DistributionPolicy:  XMallocSIMD[4096]" in s and "DistributionPolicy:  Noop" in s
+    assert "AlignmentPolicy:     Shrink[16]" in s and "OOMPolicy:           ReturnNull" in s
+
+
+def test_reference_example_config_is_rejected(ex):
+    """1 GB heap, 2 GiB access block: the reference divides by zero
+    (Scatter.hpp:991-993); the C++ API throws std::invalid_argument first."""
+    assert ex.mmcx_bad_config(0) == 1
+
+
+@pytest.mark.gpu
+def test_example01_arrays_of_arrays(ex):
+    s, g, slots, fails = ctypes.c_ulonglong(), ctypes.c_ulonglong(), ctypes.c_uint(), ctypes.c_int()
+    assert ex.mmcx_example01(0, 100, ctypes.byref(s), ctypes.byref(g), ctypes.byref(slots), ctypes.byref(fails)) == 0
+    assert fails.value == 0
+    assert s.value == g.value  # the gaussian sum n(n-1), n = threads x length
+    assert slots.value > 0
+
+
+@pytest.mark.gpu
+def test_example03_device_side_slots(ex):
+    slots = np.zeros(32, dtype=np.uint32)
+    values = np.full(32, -1, dtype=np.int32)
+    host = ctypes.c_uint()
+    assert ex.mmcx_example03(0, slots.ctypes.data, values.ctypes.data, ctypes.byref(host)) == 0
+    assert np.array_equal(values, np.arange(32))
+    # one page is formatted for 128-byte chunks, which 16-byte slots may not use
+    fresh = OracleHeap(HeapConfig(4096, 256 << 20, 16, 2, False), 1 << 30).available_slots(1)
+    assert np.all(slots == fresh - 254)
+    assert host.value == fresh - 254

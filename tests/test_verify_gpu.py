@@ -28,11 +28,31 @@ def check_live_blocks(offs, sizes, numpages, pagesize, align=16):
     return int(ok.sum())
 
 
-def assert_all_free(snap):
+def used_mask_words(ptes, masks, pagesize=4096):
+    """The on-page mask words in use: the last `segments` words of each page
+    formatted with a chunk size <= HierarchyThreshold (Scatter.hpp:397-421);
+    elsewhere the page tail is payload."""
+    ht = (pagesize - 8) // 33
+    n = masks.shape[1]
+    out = []
+    for c in np.unique(ptes[:, 0]):
+        c = int(c)
+        if c == 0 or c > ht:
+            continue
+        seg = c * 32 + 4
+        full = min(32, pagesize // seg)
+        add = min(31, ((pagesize - full * seg - 4) & 0xFFFFFFFF) // c) if full != 32 else 0
+        segments = full + (1 if add > 0 else 0)
+        rows = masks[ptes[:, 0] == c]
+        out.append(rows[:, n - segments:])
+    return np.concatenate([o.ravel() for o in out]) if out else np.zeros(0, dtype=np.uint32)
+
+
+def assert_all_free(snap, pagesize=4096):
     ptes, regions, masks, hdr = snap
     assert int(ptes[:, 1].max(initial=0)) == 0, "page fill counts not back to zero"
     assert int(ptes[:, 2].max(initial=0)) == 0, "page bitmasks not back to zero"
-    assert int(masks.max(initial=0)) == 0, "on-page masks not back to zero"
+    assert int(used_mask_words(ptes, masks, pagesize).max(initial=0)) == 0, "on-page masks not back to zero"
     assert hdr["pagebasedMutex"] == 0
 
 
