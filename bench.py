@@ -46,6 +46,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--heap-gib", type=float, default=8.0)
+    ap.add_argument("--accessblock-mib", type=int, default=2048, help="access block size (reference default 2 GiB)")
     ap.add_argument("--rounds", type=int, default=100)
     ap.add_argument("--blocks-per-sm", type=int, default=8)
     ap.add_argument("--threads", type=int, default=256)
@@ -57,13 +58,14 @@ def parse():
 
 
 def size_table(rounds: int, nthreads: int, seed: int = SEED) -> np.ndarray:
-    """u16 [rounds, nthreads]: 16 * (1 + mix64(seed, t, r) % 64)."""
+    """u16 [rounds, nthreads]: 16 * (1 + (mix64(seed, t, r) >> 32) % 64), the
+    draw the stress kernel and the CPU port make when given no table."""
     from oracle.oracle import mix64
 
     t = np.arange(nthreads, dtype=np.uint64)
     out = np.empty((rounds, nthreads), dtype=np.uint16)
     for r in range(rounds):
-        out[r] = (16 * (1 + (mix64(seed, t, r) % np.uint64(64)))).astype(np.uint16)
+        out[r] = (16 * (1 + ((mix64(seed, t, r) >> np.uint64(32)) % np.uint64(64)))).astype(np.uint16)
     return out
 
 
@@ -113,7 +115,7 @@ class ClockSampler:
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -284,7 +286,8 @@ def main():
 
     sizes_np = size_table(rounds, nthreads)
     work = algorithmic_work(sizes_np)
-    creation = CreationPolicies.Scatter(pagesize=4096, accessblocksize=2 << 30, regionsize=16, wastefactor=2)
+    creation = CreationPolicies.Scatter(pagesize=4096, accessblocksize=args.accessblock_mib << 20, regionsize=16,
+                                        wastefactor=2)
     alloc = Allocator(creation, DistributionPolicies.XMallocSIMD(4096), None, None, AlignmentPolicies.Shrink(16),
                       size=heap_bytes, device=local)
     stream = torch.cuda.current_stream()
@@ -393,7 +396,7 @@ def main():
         "config": {"workload": f"uniform_stress_{args.heap_gib:g}GiB", "heap_bytes": heap_bytes,
                    "grid": f"{sms}x{args.blocks_per_sm} blocks x {tpb} threads", "rounds": rounds,
                    "sizes": "uniform {16,32,...,1024} (u16 table in HBM)",
-                   "policies": "Scatter<4096,2GiB,16,2,noreset>+XMallocSIMD+ReturnNull+Shrink<16>",
+                   "policies": f"Scatter<4096,{args.accessblock_mib}MiB,16,2,noreset>+XMallocSIMD+ReturnNull+Shrink<16>",
                    "pairs_per_step": work["pairs"], "l2": "flushed between timed steps (512 MiB write)",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "roofline": roofline, "atomic_roofline": atomic, "cpu_baseline": cpu, "e2e": e2e,

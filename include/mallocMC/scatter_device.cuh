@@ -61,6 +61,9 @@ namespace mmc
         {
             static constexpr u32 warpSize = 32u; /* mallocMC_utils.hpp:72-73 */
             static constexpr bool coalesce = true;
+            /* read the racy first-free-block hint through L1 (it changes rarely
+             * and a stale value only moves where the search starts) */
+            static constexpr bool cachedHints = true;
             __device__ static __forceinline__ u32 laneid()
             {
                 u32 r;
@@ -86,6 +89,7 @@ namespace mmc
         {
             static constexpr u32 warpSize = 1u;
             static constexpr bool coalesce = false; /* XMallocSIMD.hpp:136-137 */
+            static constexpr bool cachedHints = false;
             __device__ static __forceinline__ u32 laneid() { return 0u; }
             __device__ static __forceinline__ u32 warpid() { return 0u; }
             __device__ static __forceinline__ u32 smid() { return 0u; }
@@ -156,24 +160,36 @@ namespace mmc
             return (spot + step) % spots;
         }
 
-        /* usespot, Scatter.hpp:329-347 (start at laneid % spots, randInit :277-281),
-         * with a retry bound: after MMC_USESPOT_MAX_TRIES lost races the word
-         * is reported full, which the callers already handle. */
-        template<class Ids>
-        __device__ __forceinline__ int usespot(u32* bitfield, u32 spots)
+        /* usespot's retry sequence (Scatter.hpp:334-346) after an atomicOr at
+         * `spot` returned `old` with that bit already set: stop when the word is
+         * full, else try the next free spot of the returned word. Bounded by
+         * MMC_USESPOT_MAX_TRIES lost races, after which the word counts as full,
+         * which every caller already handles. */
+        __device__ __forceinline__ int usespot_continue(u32* bitfield, u32 spots, u32 spot, u32 old)
         {
-            u32 spot = Ids::laneid() % spots;
-            for(u32 it = 0; it < MMC_USESPOT_MAX_TRIES; ++it)
+            for(u32 it = 1; it < MMC_USESPOT_MAX_TRIES; ++it)
             {
-                const u32 mask = 1u << spot;
-                const u32 old = atomicOr(bitfield, mask);
-                if((old & mask) == 0u)
-                    return static_cast<int>(spot);
                 if(static_cast<u32>(__popc(old)) >= spots)
                     return -1;
                 spot = nextspot(old, spot, spots);
+                const u32 mask = 1u << spot;
+                old = atomicOr(bitfield, mask);
+                if((old & mask) == 0u)
+                    return static_cast<int>(spot);
             }
             return -1;
+        }
+
+        /* usespot, Scatter.hpp:329-347 (first spot laneid % spots, randInit :277-281) */
+        template<class Ids>
+        __device__ __forceinline__ int usespot(u32* bitfield, u32 spots)
+        {
+            const u32 spot = Ids::laneid() % spots;
+            const u32 mask = 1u << spot;
+            const u32 old = atomicOr(bitfield, mask);
+            if((old & mask) == 0u)
+                return static_cast<int>(spot);
+            return usespot_continue(bitfield, spots, spot, old);
         }
 
         /* calcAdditionalChunks, Scatter.hpp:365-381: the (int) casts collapse to
@@ -186,58 +202,98 @@ namespace mmc
             return 0u;
         }
 
-        /* Capacity of a page formatted with chunksize (countFreeChunksInPage's
-         * capacity term, Scatter.hpp:1116-1138; tryUsePage's bound, :493-508). */
-        __device__ __forceinline__ u32 page_capacity(const mmc_device_handle& h, u32 chunksize)
+        /* Geometry of a page formatted with a chunk size (tryUsePage :493-508,
+         * deallocChunked :652-660, countFreeChunksInPage :1116-1138). */
+        struct ChunkGeom
         {
-            if(chunksize <= h.hierarchyThreshold)
+            bool hier;        /* chunksize <= HierarchyThreshold: on-page segment masks */
+            u32 fullsegments; /* hierarchical: segments of 32 chunks */
+            u32 additional;   /* hierarchical: chunks in the last, partial segment */
+            u32 segments;     /* hierarchical: on-page mask words */
+            u32 capacity;     /* chunks the page holds */
+        };
+
+        __device__ __forceinline__ ChunkGeom chunk_geom(const mmc_device_handle& h, u32 chunksize)
+        {
+            ChunkGeom g;
+            g.hier = chunksize <= h.hierarchyThreshold;
+            if(g.hier)
             {
                 const u32 segmentsize = chunksize * 32u + 4u;
-                const u32 fullsegments = umin(32u, h.pagesize / segmentsize);
-                return fullsegments * 32u + calc_additional_chunks(h.pagesize, fullsegments, segmentsize, chunksize);
+                g.fullsegments = umin(32u, h.pagesize / segmentsize);
+                g.additional = calc_additional_chunks(h.pagesize, g.fullsegments, segmentsize, chunksize);
+                g.segments = g.fullsegments + (g.additional > 0u ? 1u : 0u);
+                g.capacity = g.fullsegments * 32u + g.additional;
             }
-            return umin(h.pagesize / chunksize, 32u);
+            else
+            {
+                g.fullsegments = g.additional = g.segments = 0u;
+                g.capacity = umin(h.pagesize / chunksize, 32u);
+            }
+            return g;
         }
 
-        /* addChunkHierarchy, Scatter.hpp:397-421 */
-        template<class Ids>
-        __device__ void* add_chunk_hierarchy(const mmc_device_handle& h, u32 chunksize, u32 fullsegments,
-                                             u32 additional_chunks, u32 page)
+        /* Capacity of a page formatted with chunksize. */
+        __device__ __forceinline__ u32 page_capacity(const mmc_device_handle& h, u32 chunksize)
         {
-            const u32 segments = fullsegments + (additional_chunks > 0u ? 1u : 0u);
-            u32 spot = Ids::laneid() % segments;
-            const u32 mask = ld_rlx(&h.bitmask[page]);
-            if((mask & (1u << spot)) != 0u)
-                spot = nextspot(mask, spot, segments);
-            const u32 tries = segments - static_cast<u32>(__popc(mask));
-            u32* onpagemasks = on_page_masks(h, page, segments);
-            for(u32 i = 0; i < tries; ++i)
+            return chunk_geom(h, chunksize).capacity;
+        }
+
+        /* Claim one chunk on a page whose fill slot is reserved:
+         * addChunkHierarchy (Scatter.hpp:397-421) for hierarchical pages,
+         * addChunkNoHierarchy (:432-443) otherwise. Both begin with one atomicOr
+         * on a per-lane word (a segment's on-page mask or the page bitmask), so
+         * the lanes of a warp issue that first claim as a single instruction
+         * whatever their page kind; a lane that loses the race continues the
+         * reference's exact retry sequence. `mask` is the page's segment hints. */
+        template<class Ids>
+        __device__ void* claim_chunk(const mmc_device_handle& h, u32 page, u32 chunksize, const ChunkGeom& g, u32 mask)
+        {
+            u32* word;
+            u32 spots;
+            u32 seg = 0u;
+            u32 tries = 1u;
+            u32* onpagemasks = nullptr;
+            if(g.hier)
             {
-                const u32 spots = spot < fullsegments ? 32u : additional_chunks;
-                const int hspot = usespot<Ids>(&onpagemasks[spot], spots);
-                if(hspot != -1)
-                    return page_data(h, page) + (32u * spot + static_cast<u32>(hspot)) * chunksize;
-                atomicOr(&h.bitmask[page], 1u << spot);
+                seg = Ids::laneid() % g.segments;
+                if((mask & (1u << seg)) != 0u)
+                    seg = nextspot(mask, seg, g.segments);
+                tries = g.segments - static_cast<u32>(__popc(mask));
+                onpagemasks = on_page_masks(h, page, g.segments);
+                word = onpagemasks + seg;
+                spots = seg < g.fullsegments ? 32u : g.additional;
+            }
+            else
+            {
+                word = &h.bitmask[page];
+                spots = g.capacity;
+            }
+            if(tries == 0u)
+                return nullptr;
+            const u32 spot = Ids::laneid() % spots;
+            const u32 bit = 1u << spot;
+            const u32 old = atomicOr(word, bit);
+            int got = (old & bit) == 0u ? static_cast<int>(spot) : usespot_continue(word, spots, spot, old);
+            if(!g.hier)
+                return got == -1 ? nullptr : page_data(h, page) + static_cast<u32>(got) * chunksize;
+            for(u32 i = 0;;)
+            {
+                if(got != -1)
+                    return page_data(h, page) + (32u * seg + static_cast<u32>(got)) * chunksize;
+                atomicOr(&h.bitmask[page], 1u << seg);
                 /* A free in this segment may have cleared the hint just before
                  * it was set; undo a mark the segment no longer deserves so no
                  * stale "full" bit outlives the chunks. A lone thread only gets
                  * here for a full segment, so this never fires serially. */
-                if(static_cast<u32>(__popc(ld_rlx(&onpagemasks[spot]))) < spots)
-                    atomicAnd(&h.bitmask[page], ~(1u << spot));
-                spot = nextspot(mask, spot, segments);
+                if(static_cast<u32>(__popc(ld_rlx(&onpagemasks[seg]))) < spots)
+                    atomicAnd(&h.bitmask[page], ~(1u << seg));
+                seg = nextspot(mask, seg, g.segments);
+                if(++i >= tries)
+                    return nullptr;
+                spots = seg < g.fullsegments ? 32u : g.additional;
+                got = usespot<Ids>(&onpagemasks[seg], spots);
             }
-            return nullptr;
-        }
-
-        /* addChunkNoHierarchy, Scatter.hpp:432-443 */
-        template<class Ids>
-        __device__ __forceinline__ void* add_chunk_no_hierarchy(const mmc_device_handle& h, u32 chunksize, u32 page,
-                                                                u32 spots)
-        {
-            const int spot = usespot<Ids>(&h.bitmask[page], spots);
-            if(spot == -1)
-                return nullptr;
-            return page_data(h, page) + static_cast<u32>(spot) * chunksize;
         }
 
         /* tryUsePage, Scatter.hpp:454-518; [lo, hi] is isChunkSizeInRange (:586-588). */
@@ -245,6 +301,10 @@ namespace mmc
         __device__ void* try_use_page(const mmc_device_handle& h, u32 page, u32 chunksize, u32 lo, u32 hi)
         {
             void* chunk_ptr = nullptr;
+            /* the segment hints are read before the fill-count atomic so both
+             * round trips overlap (the reference reads them just after it,
+             * Scatter.hpp:404; alone on the heap both reads see the same word) */
+            u32 mask = chunksize <= h.hierarchyThreshold ? ld_rlx(&h.bitmask[page]) : 0u;
             const u32 filllevel = atomicAdd(&h.count[page], 1u);
             bool tryAllocMem = !h.resetfreedpages;
             if(h.resetfreedpages && filllevel < h.pagesize)
@@ -252,50 +312,53 @@ namespace mmc
                 const u32 oldChunksize = atomicCAS(&h.chunksize[page], 0u, chunksize);
                 if(oldChunksize == 0u || (oldChunksize >= lo && oldChunksize <= hi))
                     tryAllocMem = true;
-                if(oldChunksize != 0u)
+                if(oldChunksize != 0u && oldChunksize != chunksize)
+                {
                     chunksize = oldChunksize;
+                    mask = ld_rlx(&h.bitmask[page]);
+                }
             }
             if(tryAllocMem)
             {
-                if(chunksize <= h.hierarchyThreshold)
-                {
-                    const u32 segmentsize = chunksize * 32u + 4u;
-                    const u32 fullsegments = umin(32u, h.pagesize / segmentsize);
-                    const u32 additional_chunks
-                        = calc_additional_chunks(h.pagesize, fullsegments, segmentsize, chunksize);
-                    if(filllevel < fullsegments * 32u + additional_chunks)
-                        chunk_ptr = add_chunk_hierarchy<Ids>(h, chunksize, fullsegments, additional_chunks, page);
-                }
-                else
-                {
-                    const u32 chunksinpage = umin(h.pagesize / chunksize, 32u);
-                    if(filllevel < chunksinpage)
-                        chunk_ptr = add_chunk_no_hierarchy<Ids>(h, chunksize, page, chunksinpage);
-                }
+                const ChunkGeom g = chunk_geom(h, chunksize);
+                if(filllevel < g.capacity)
+                    chunk_ptr = claim_chunk<Ids>(h, page, chunksize, g, mask);
             }
             if(chunk_ptr == nullptr)
                 atomicSub(&h.count[page], 1u);
             return chunk_ptr;
         }
 
-        /* allocChunked, Scatter.hpp:527-637 */
+        /* One page of allocChunked's walk (Scatter.hpp:580-604), given the page's
+         * chunk size as already loaded. The reference's CAS(0 -> minAllocation)
+         * only writes a zero word; on a formatted page it just returns the value,
+         * so it is issued only when the load saw zero. */
         template<class Ids>
-        __device__ void* alloc_chunked(const mmc_device_handle& h, u32 bytes)
+        __device__ __forceinline__ void* attempt_page(const mmc_device_handle& h, u32 page, u32 before, u32 bytes,
+                                                      u32 minAllocation, u32 maxchunksize)
         {
-            const u32 P = h.pagesize;
+            if(before == 0u)
+                before = atomicCAS(&h.chunksize[page], 0u, minAllocation);
+            u32 use = 0u;
+            if(before == 0u)
+                use = minAllocation;
+            else if(before >= bytes && before <= maxchunksize)
+                use = before;
+            if(use == 0u)
+                return nullptr;
+            return try_use_page<Ids>(h, page, use, bytes, maxchunksize);
+        }
+
+        /* allocChunked's two-pass region walk (Scatter.hpp:563-636), resumed after
+         * the first page: in the first region of pass 0 the region counter is
+         * the one already read (fill0) and the start page was already tried. */
+        template<class Ids>
+        __device__ void* alloc_chunked_walk(const mmc_device_handle& h, u32 bytes, u32 minAllocation,
+                                            u32 maxchunksize, u32 global_start_page, u32 fill0)
+        {
             const u32 R = h.regionsize;
-            const u32 minAllocation = umax(bytes, h.paddedMinChunkSize);
             const u32 numpages = h.numpages;
             const u32 pagesperblock = h.pagesperblock;
-            const u32 reloff = Ids::warpSize * minAllocation / P;
-            const u32 start_page_in_block = (minAllocation * h.hashingK + h.hashingDistMP * Ids::smid()
-                                             + (h.hashingDistWP + h.hashingDistWPRel * reloff) * Ids::warpid())
-                % pagesperblock;
-            const u32 maxchunksize = umin(P, umax(h.wastefactor * bytes, h.paddedMinChunkSize));
-            u32 global_start_page = start_page_in_block + ld_rlx(&h.state->firstfreeblock) * pagesperblock;
-            if(global_start_page >= numpages)
-                global_start_page %= numpages; /* unreachable for a consistent header; keeps accesses in bounds */
-
             u32 checklevel = R * 3u / 4u;
             for(u32 finder = 0; finder < 2u; ++finder)
             {
@@ -303,25 +366,23 @@ namespace mmc
                 do
                 {
                     const u32 region = global_page / R;
-                    const u32 regionfilllevel = ld_rlx(&h.regions[region]);
+                    const bool resumed = finder == 0u && global_page == global_start_page;
+                    const u32 regionfilllevel = resumed ? fill0 : ld_rlx(&h.regions[region]);
                     const u32 region_offset = region * R;
                     if(regionfilllevel < checklevel)
                     {
                         u32 page_in_region = global_page;
+                        bool skip = resumed;
                         do
                         {
-                            const u32 beforeChunkSize = atomicCAS(&h.chunksize[page_in_region], 0u, minAllocation);
-                            u32 useChunkSize = 0u;
-                            if(beforeChunkSize == 0u)
-                                useChunkSize = minAllocation;
-                            else if(beforeChunkSize >= bytes && beforeChunkSize <= maxchunksize)
-                                useChunkSize = beforeChunkSize;
-                            if(useChunkSize != 0u)
+                            if(!skip)
                             {
-                                void* res = try_use_page<Ids>(h, page_in_region, useChunkSize, bytes, maxchunksize);
+                                void* res = attempt_page<Ids>(h, page_in_region, ld_rlx(&h.chunksize[page_in_region]),
+                                                              bytes, minAllocation, maxchunksize);
                                 if(res != nullptr)
                                     return res;
                             }
+                            skip = false;
                             page_in_region = region_offset + ((page_in_region + 1u) % R);
                         } while(page_in_region != global_page);
 
@@ -342,29 +403,57 @@ namespace mmc
             return nullptr;
         }
 
+        /* allocChunked, Scatter.hpp:527-637. The walk's first page is tried with
+         * its region counter and chunk size read together, as straight-line
+         * code every lane of a warp executes in step; only lanes whose first
+         * page fails enter the (divergent) rest of the walk. */
+        template<class Ids>
+        __device__ void* alloc_chunked(const mmc_device_handle& h, u32 bytes)
+        {
+            const u32 P = h.pagesize;
+            const u32 R = h.regionsize;
+            const u32 minAllocation = umax(bytes, h.paddedMinChunkSize);
+            const u32 numpages = h.numpages;
+            const u32 pagesperblock = h.pagesperblock;
+            const u32 reloff = Ids::warpSize * minAllocation / P;
+            const u32 start_page_in_block = (minAllocation * h.hashingK + h.hashingDistMP * Ids::smid()
+                                             + (h.hashingDistWP + h.hashingDistWPRel * reloff) * Ids::warpid())
+                % pagesperblock;
+            const u32 maxchunksize = umin(P, umax(h.wastefactor * bytes, h.paddedMinChunkSize));
+            const u32 ffb = Ids::cachedHints ? __ldca(&h.state->firstfreeblock) : ld_rlx(&h.state->firstfreeblock);
+            u32 global_start_page = start_page_in_block + ffb * pagesperblock;
+            if(global_start_page >= numpages)
+                global_start_page %= numpages; /* unreachable for a consistent header; keeps accesses in bounds */
+
+            const u32 fill0 = ld_rlx(&h.regions[global_start_page / R]);
+            const u32 cs0 = ld_rlx(&h.chunksize[global_start_page]);
+            if(fill0 < R * 3u / 4u)
+            {
+                void* res = attempt_page<Ids>(h, global_start_page, cs0, bytes, minAllocation, maxchunksize);
+                if(res != nullptr)
+                    return res;
+            }
+            return alloc_chunked_walk<Ids>(h, bytes, minAllocation, maxchunksize, global_start_page, fill0);
+        }
+
         /* deallocChunked, Scatter.hpp:646-736 */
         template<class Ids>
         __device__ void dealloc_chunked(const mmc_device_handle& h, void* mem, u32 page, u32 chunksize)
         {
             const u32 P = h.pagesize;
             const u32 inpage_offset = static_cast<u32>(static_cast<char*>(mem) - page_data(h, page));
+            u32 segment;
             if(chunksize <= h.hierarchyThreshold)
             {
-                const u32 segmentsize = chunksize * 32u + 4u;
-                const u32 fullsegments = umin(32u, P / segmentsize);
-                const u32 additional_chunks = calc_additional_chunks(P, fullsegments, segmentsize, chunksize);
-                const u32 segment = inpage_offset / (chunksize * 32u);
+                const ChunkGeom g = chunk_geom(h, chunksize);
+                segment = inpage_offset / (chunksize * 32u);
                 const u32 withinsegment = (inpage_offset - segment * (chunksize * 32u)) / chunksize;
-                const u32 nMasks = fullsegments + (additional_chunks > 0u ? 1u : 0u);
-                u32* onpagemasks = on_page_masks(h, page, nMasks);
-                atomicAnd(&onpagemasks[segment], ~(1u << withinsegment));
-                atomicAnd(&h.bitmask[page], ~(1u << segment));
+                atomicAnd(on_page_masks(h, page, g.segments) + segment, ~(1u << withinsegment));
             }
             else
-            {
-                const u32 segment = inpage_offset / chunksize;
-                atomicAnd(&h.bitmask[page], ~(1u << segment));
-            }
+                segment = inpage_offset / chunksize;
+            /* both kinds clear their bit of the page bitmask (:665, :670) */
+            atomicAnd(&h.bitmask[page], ~(1u << segment));
 
             u32 oldfilllevel = 0u;
             if(h.resetfreedpages)
@@ -536,6 +625,12 @@ namespace mmc
             return alloc_page_based<Ids>(h, bytes);
         }
 
+        /* 64-bit division for page sizes that are not powers of two, kept out of line */
+        __device__ __noinline__ inline u32 page_of_offset_slow(u64 offset, u32 pagesize)
+        {
+            return static_cast<u32>(offset / pagesize);
+        }
+
         /* destroy, Scatter.hpp:918-946. A pointer outside the pool or on a page
          * without a chunk size (where the reference would divide by zero) is
          * recorded as MMC_DEVERR_BADFREE and ignored. */
@@ -552,7 +647,7 @@ namespace mmc
                 return;
             }
             const u32 page = (P & (P - 1u)) == 0u ? static_cast<u32>(offset >> (__ffs(static_cast<int>(P)) - 1))
-                                                  : static_cast<u32>(offset / P);
+                                                  : page_of_offset_slow(offset, P);
             const u32 chunksize = ld_rlx(&h.chunksize[page]);
             if(chunksize == 0u)
             {

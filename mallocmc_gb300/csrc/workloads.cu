@@ -65,7 +65,8 @@ __global__ void __launch_bounds__(256) mmc_stress_kernel(mmc_device_handle h, mm
     for(uint32_t r = 0; r < p.rounds; ++r)
     {
         const uint64_t m = mix64(p.seed, t, r);
-        const uint32_t bytes = sizes ? sizes[r * nthreads + t] : p.lo + static_cast<uint32_t>(m % nsizes) * p.step;
+        const uint32_t bytes
+            = sizes ? sizes[r * nthreads + t] : p.lo + (static_cast<uint32_t>(m >> 32) % nsizes) * p.step;
         char* ptr = static_cast<char*>(dv::malloc<dv::GpuIds>(h, bytes));
         if(ptr == nullptr)
         {

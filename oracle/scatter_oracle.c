@@ -756,7 +756,7 @@ static void* stress_worker(void* arg)
         for(uint32_t r = 0; r < s->rounds; ++r)
         {
             const uint64_t m = oc_mix64(s->seed, t, r);
-            const uint32_t bytes = s->lo + (uint32_t) (m % nsizes) * s->step;
+            const uint32_t bytes = s->lo + ((uint32_t) (m >> 32) % nsizes) * s->step;
             uint64_t* p = (uint64_t*) oc_malloc(s->h, bytes);
             if(!p)
             {
