@@ -47,7 +47,15 @@ struct mmc_heap_state
     uint32_t pad2[31];
     uint32_t error_flags; /* MMC_DEVERR_* */
     uint32_t pad3[31];
+    /* event counters, maintained only in builds with MMC_DEVICE_STATS (MMC_STAT_*) */
+    unsigned long long stats[16];
 };
+
+#ifdef MMC_DEVICE_STATS
+#define MMC_STAT(h, i) atomicAdd(&(h).state->stats[(i)], 1ull)
+#else
+#define MMC_STAT(h, i) ((void) 0)
+#endif
 
 namespace mmc
 {
@@ -345,8 +353,14 @@ namespace mmc
             else if(before >= bytes && before <= maxchunksize)
                 use = before;
             if(use == 0u)
+            {
+                MMC_STAT(h, MMC_STAT_SIZE_MISMATCH);
                 return nullptr;
-            return try_use_page<Ids>(h, page, use, bytes, maxchunksize);
+            }
+            void* r = try_use_page<Ids>(h, page, use, bytes, maxchunksize);
+            if(r == nullptr)
+                MMC_STAT(h, MMC_STAT_PAGE_FULL);
+            return r;
         }
 
         /* allocChunked's two-pass region walk (Scatter.hpp:563-636), resumed after
@@ -377,6 +391,7 @@ namespace mmc
                         {
                             if(!skip)
                             {
+                                MMC_STAT(h, MMC_STAT_WALK_PAGES);
                                 void* res = attempt_page<Ids>(h, page_in_region, ld_rlx(&h.chunksize[page_in_region]),
                                                               bytes, minAllocation, maxchunksize);
                                 if(res != nullptr)
@@ -388,7 +403,10 @@ namespace mmc
 
                         if(regionfilllevel + 1u <= R)
                             atomicCAS(&h.regions[region], regionfilllevel, regionfilllevel + 1u);
+                        MMC_STAT(h, MMC_STAT_REGION_FAIL);
                     }
+                    else
+                        MMC_STAT(h, MMC_STAT_REGION_SKIP);
                     global_page = (global_page + R) % numpages;
                     if(global_page % pagesperblock == 0u)
                     {
@@ -427,13 +445,20 @@ namespace mmc
 
             const u32 fill0 = ld_rlx(&h.regions[global_start_page / R]);
             const u32 cs0 = ld_rlx(&h.chunksize[global_start_page]);
+            MMC_STAT(h, MMC_STAT_CHUNKED);
             if(fill0 < R * 3u / 4u)
             {
                 void* res = attempt_page<Ids>(h, global_start_page, cs0, bytes, minAllocation, maxchunksize);
                 if(res != nullptr)
+                {
+                    MMC_STAT(h, MMC_STAT_FIRST_PAGE);
                     return res;
+                }
             }
-            return alloc_chunked_walk<Ids>(h, bytes, minAllocation, maxchunksize, global_start_page, fill0);
+            void* res = alloc_chunked_walk<Ids>(h, bytes, minAllocation, maxchunksize, global_start_page, fill0);
+            if(res == nullptr)
+                MMC_STAT(h, MMC_STAT_CHUNKED_FAIL);
+            return res;
         }
 
         /* deallocChunked, Scatter.hpp:646-736 */
@@ -622,6 +647,7 @@ namespace mmc
                 return nullptr;
             if(bytes <= h.pagesize)
                 return alloc_chunked<Ids>(h, bytes);
+            MMC_STAT(h, MMC_STAT_PAGE_BASED);
             return alloc_page_based<Ids>(h, bytes);
         }
 
@@ -739,7 +765,15 @@ namespace mmc
             void* mem = create<Ids>(h, req);
             mem = handle_oom(h, mem, req);
             if(coalescible && lane == leader && mem != nullptr)
-                *static_cast<u32*>(mem) = threadcount;
+            {
+                /* The lane count must reach L2 before any sub-allocation can be
+                 * freed: the frees are device-scope atomicSubs on this word and
+                 * are ordered after the broadcast below, which follows the fence.
+                 * (The reference stores it with a block-scope fence only,
+                 * XMallocSIMD.hpp:160-166.) */
+                st_rlx(static_cast<u32*>(mem), threadcount);
+                __threadfence();
+            }
             const unsigned long long base
                 = __shfl_sync(active, reinterpret_cast<unsigned long long>(mem), static_cast<int>(leader));
             if(!coalescible)

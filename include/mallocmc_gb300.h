@@ -50,6 +50,19 @@ typedef enum mmc_status
 #define MMC_DEVERR_BADFREE 0x2u  /* free of a pointer outside the heap or on an unformatted page */
 #define MMC_DEVERR_OOM 0x4u      /* an allocation failed under MMC_OOM_FLAG */
 
+/* Device event counters (mmc_heap_stats); maintained only when the library is
+ * built with MMC_DEVICE_STATS, zero otherwise. */
+#define MMC_STAT_CHUNKED 0       /* chunked allocations started (allocChunked calls) */
+#define MMC_STAT_FIRST_PAGE 1    /* ... served by the walk's first page */
+#define MMC_STAT_WALK_PAGES 2    /* further pages tried by the walk */
+#define MMC_STAT_REGION_FAIL 3   /* regions walked without success (region counter bumps) */
+#define MMC_STAT_REGION_SKIP 4   /* regions skipped as 3/4 full (pass 0) or full */
+#define MMC_STAT_SIZE_MISMATCH 5 /* pages tried whose chunk size did not fit the request */
+#define MMC_STAT_PAGE_FULL 6     /* pages tried whose chunks were all taken */
+#define MMC_STAT_CHUNKED_FAIL 7  /* chunked allocations that returned NULL */
+#define MMC_STAT_PAGE_BASED 8    /* multi-page allocations started */
+#define MMC_STAT_COUNT 16
+
 /* Heap configuration: the template parameters of Scatter<HeapConfig, HashConfig>
  * (creationPolicies/Scatter.hpp:56-85, 124-207), XMallocSIMD<Config> and
  * Shrink<Config> (alignmentPolicies/Shrink.hpp:62-65) as runtime values. */
@@ -180,6 +193,12 @@ mmc_status mmc_available_slots_async(mmc_heap* heap, size_t slot_size, void* str
 /* Device error bits (MMC_DEVERR_*) accumulated since the last clear; waits for
  * `stream`. clear != 0 resets them. */
 mmc_status mmc_heap_error(mmc_heap* heap, void* stream, uint32_t* flags, int clear);
+
+/* Device event counters (MMC_STAT_*, MMC_STAT_COUNT values) into out; waits for
+ * `stream`; clear != 0 zeroes them. The counters implement the survey-planned
+ * allocator statistics (pages scanned, walk failures); they have no counterpart
+ * in the reference and are maintained only in MMC_DEVICE_STATS builds. */
+mmc_status mmc_heap_stats(mmc_heap* heap, void* stream, unsigned long long* out, int clear);
 
 /* Copy the metadata to host buffers (each may be NULL): ptes3 = numpages x
  * {chunksize, count, bitmask}; regions = numregions words; masks = numpages x

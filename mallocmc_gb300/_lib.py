@@ -70,6 +70,7 @@ SIGNATURES = {
     "mmc_available_slots_async": (ctypes.c_int, [vp, ctypes.c_size_t, vp, vp]),
     "mmc_heap_error": (ctypes.c_int, [vp, vp, ctypes.POINTER(u32), ctypes.c_int]),
     "mmc_snapshot_metadata": (ctypes.c_int, [vp, vp, vp, vp, vp, vp]),
+    "mmc_heap_stats": (ctypes.c_int, [vp, vp, vp, ctypes.c_int]),
     "mmc_last_error": (ctypes.c_char_p, []),
     "mmc_run_program": (ctypes.c_int, [vp, vp, vp, i64, vp, vp]),
     "mmc_run_stress": (ctypes.c_int, [vp, ctypes.POINTER(MmcStressParams), vp, vp, vp]),

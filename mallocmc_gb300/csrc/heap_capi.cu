@@ -341,6 +341,8 @@ namespace
         const mmc_geometry& g = h->geom;
         st = cuda_check(cudaMemsetAsync(h->pool + g.ptes_offset, 0, 12ull * g.numpages + 4ull * g.numregions, s),
                         "zero page table");
+        if(st == MMC_OK)
+            st = cuda_check(cudaMemsetAsync(h->state, 0, sizeof(mmc_heap_state), s), "zero heap header");
         if(st != MMC_OK)
             return st;
         const uint64_t words = static_cast<uint64_t>(g.numpages) * g.maxOnPageMasks;
@@ -630,6 +632,21 @@ mmc_status mmc_heap_error(mmc_heap* h, void* stream, uint32_t* flags, int clear)
         if(st == MMC_OK)
             st = cuda_check(cudaStreamSynchronize(s), "wait for clear");
     }
+    return st;
+}
+
+mmc_status mmc_heap_stats(mmc_heap* h, void* stream, unsigned long long* out, int clear)
+{
+    if(h == nullptr || out == nullptr)
+        return fail(MMC_ERR_ARG, "null argument");
+    cudaStream_t s = as_stream(stream);
+    mmc_status st = cuda_check(cudaStreamSynchronize(s), "synchronise before stats");
+    if(st == MMC_OK)
+        st = cuda_check(cudaMemcpy(out, h->state->stats, sizeof(unsigned long long) * MMC_STAT_COUNT,
+                                   cudaMemcpyDeviceToHost),
+                        "copy stats");
+    if(st == MMC_OK && clear)
+        st = cuda_check(cudaMemset(h->state->stats, 0, sizeof(unsigned long long) * MMC_STAT_COUNT), "clear stats");
     return st;
 }
 

@@ -186,3 +186,24 @@ def test_page_based_allocations_concurrent():
         assert int(ptes[:, 0].max()) <= 4096  # every multi-page run released
         assert_all_free((ptes, regions, masks, hdr))
         assert alloc.error_flags() == 0
+
+
+def test_stress_full_size_steps_no_corruption():
+    """The benchmark workload (8 GiB heap, SMs x 8 x 256 threads, 100 rounds of
+    malloc / u64 pattern / verify / free) three times back to back: no block may
+    ever be handed out twice (a pattern error), none may fail, and everything
+    must be free afterwards."""
+    import torch
+
+    from mallocmc_gb300.workloads import run_stress
+
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    cfg = HeapConfig(4096, 2 << 30, 16, 2, False)
+    with gpu_allocator(cfg, 8 << 30) as alloc:
+        for step in range(3):
+            st = run_stress(alloc, sms * 8, 256, 100, 16, 1024, 16, seed=100 + step)
+            assert st["pairs"] == sms * 8 * 256 * 100, st
+            assert st["nulls"] == 0 and st["bad"] == 0, st
+        snap = alloc.snapshot()
+        assert_all_free(snap)
+        assert alloc.error_flags() == 0
