@@ -188,6 +188,27 @@ mmc_status mmc_available_slots(mmc_heap* heap, size_t slot_size, void* stream, u
  * capture in a CUDA graph once the heap exists. */
 mmc_status mmc_available_slots_async(mmc_heap* heap, size_t slot_size, void* stream, unsigned* out_dev);
 
+/* Free-slot count that allocates nothing, for callers that cannot call
+ * cudaMalloc: code running while a CUDA graph is being captured (a global-mode
+ * capture refuses cudaMalloc), and code inside a framework whose device memory
+ * belongs to its own pool allocator, which holds only a device handle and must
+ * not take memory behind the pool's back. It needs no mmc_heap, only the
+ * handle: the scan's partial sums live in one file-scope __device__ array of
+ * MMC_NOALLOC_SCAN_BLOCKS_MAX entries (16 bytes each, 32 KiB in all), which every
+ * GPU that loads the library holds until the process exits. The count is
+ * written to *out_dev (device memory) when `stream` reaches it.
+ * scan_blocks = 0 picks 4 x the SM count; more than MMC_NOALLOC_SCAN_BLOCKS_MAX
+ * is rejected with MMC_ERR_ARG. The calling thread's current device must be
+ * the heap's. The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress), so make that first call before any stream capture.
+ * Every call shares the array: calls that overlap on the GPU (on two streams,
+ * say) race and may return wrong counts. Each call rewrites every entry it
+ * reads, so nothing carries over from the last call. This entry point has no
+ * counterpart in the reference. */
+#define MMC_NOALLOC_SCAN_BLOCKS_MAX 2048
+mmc_status mmc_available_slots_noalloc(const mmc_device_handle* handle, size_t slot_size, unsigned scan_blocks,
+                                       void* stream, unsigned* out_dev);
+
 /* --------------------------------------------------------- introspection */
 
 /* Device error bits (MMC_DEVERR_*) accumulated since the last clear; waits for

@@ -68,6 +68,8 @@ SIGNATURES = {
     "mmc_heap_info": (ctypes.c_int, [vp, ctypes.c_char_p, ctypes.c_size_t]),
     "mmc_available_slots": (ctypes.c_int, [vp, ctypes.c_size_t, vp, ctypes.POINTER(ctypes.c_uint)]),
     "mmc_available_slots_async": (ctypes.c_int, [vp, ctypes.c_size_t, vp, vp]),
+    "mmc_available_slots_noalloc": (ctypes.c_int, [ctypes.POINTER(MmcDeviceHandle), ctypes.c_size_t, ctypes.c_uint,
+                                                   vp, vp]),
     "mmc_heap_error": (ctypes.c_int, [vp, vp, ctypes.POINTER(u32), ctypes.c_int]),
     "mmc_snapshot_metadata": (ctypes.c_int, [vp, vp, vp, vp, vp, vp]),
     "mmc_heap_stats": (ctypes.c_int, [vp, vp, vp, ctypes.c_int]),

@@ -20,6 +20,7 @@
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <sstream>
 #include <string>
@@ -219,6 +220,19 @@ __global__ void mmc_slots_pass2(const SlotPartial* partials, uint32_t nparts, ui
     if(lane == 0)
         *out = mmc::dev::run_total(s, n);
 }
+
+/* Scratch of mmc_available_slots_noalloc: one scan partial per block. Every
+ * GPU that loads the library holds it (32 KiB) until the process exits; in host
+ * code the name is not a device address, so it is reached only through the
+ * address cudaGetSymbolAddress returns for the current device. */
+static __device__ __align__(256) SlotPartial g_noalloc_partials[MMC_NOALLOC_SCAN_BLOCKS_MAX];
+
+namespace
+{
+    constexpr int kNoallocMaxDevices = 64;
+    std::mutex g_noalloc_mutex;
+    SlotPartial* g_noalloc_addr[kNoallocMaxDevices] = {};
+} // namespace
 
 /* ------------------------------------------------------------- host logic */
 
@@ -591,6 +605,48 @@ mmc_status mmc_available_slots_async(mmc_heap* h, size_t slot_size, void* stream
         return fail(MMC_ERR_ARG, "null argument");
     const uint32_t slot = mmc::dev::apply_padding(h->cfg.dataAlignment, static_cast<uint32_t>(slot_size));
     return launch_available_slots(h, slot, as_stream(stream), out_dev);
+}
+
+mmc_status mmc_available_slots_noalloc(const mmc_device_handle* handle, size_t slot_size, unsigned scan_blocks,
+                                       void* stream, unsigned* out_dev)
+{
+    if(handle == nullptr || out_dev == nullptr)
+        return fail(MMC_ERR_ARG, "null argument");
+    int dev = 0;
+    mmc_status st = cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
+    if(st != MMC_OK)
+        return st;
+    if(dev < 0 || dev >= kNoallocMaxDevices)
+        return fail(MMC_ERR_ARG, "device ordinal beyond the no-alloc entry point's table");
+    if(scan_blocks == 0u)
+        scan_blocks = scan_grid(dev);
+    if(scan_blocks > MMC_NOALLOC_SCAN_BLOCKS_MAX)
+        return fail(MMC_ERR_ARG, "scan_blocks " + std::to_string(scan_blocks) + " exceeds the static scratch of "
+                                     + std::to_string(MMC_NOALLOC_SCAN_BLOCKS_MAX) + " partials");
+    SlotPartial* partials = nullptr;
+    {
+        /* set-up, once per device, with that device current */
+        std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+        if(g_noalloc_addr[dev] == nullptr)
+        {
+            void* p = nullptr;
+            st = cuda_check(cudaGetSymbolAddress(&p, g_noalloc_partials), "cudaGetSymbolAddress");
+            if(st != MMC_OK)
+                return st;
+            g_noalloc_addr[dev] = static_cast<SlotPartial*>(p);
+        }
+        partials = g_noalloc_addr[dev];
+    }
+    const uint32_t slot = mmc::dev::apply_padding(handle->dataAlignment, static_cast<uint32_t>(slot_size));
+    const bool multi = slot >= handle->pagesize;
+    cudaStream_t s = as_stream(stream);
+    if(multi)
+        mmc_slots_pass1<true><<<scan_blocks, kScanThreads, 0, s>>>(*handle, slot, partials);
+    else
+        mmc_slots_pass1<false><<<scan_blocks, kScanThreads, 0, s>>>(*handle, slot, partials);
+    const uint32_t n = (slot + handle->pagesize - 1u) / handle->pagesize;
+    mmc_slots_pass2<<<1, 32, 0, s>>>(partials, scan_blocks, multi ? 1u : 0u, n, out_dev);
+    return cuda_check(cudaGetLastError(), "no-alloc slot count kernels");
 }
 
 mmc_status mmc_available_slots(mmc_heap* h, size_t slot_size, void* stream, unsigned* out)
