@@ -46,14 +46,22 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--heap-gib", type=float, default=8.0)
-    ap.add_argument("--accessblock-mib", type=int, default=2048, help="access block size (reference default 2 GiB)")
+    ap.add_argument("--accessblock-mib", type=int, default=4096,
+                    help="access block size; 4096 (two blocks on 8 GiB) is the autotuned choice for this workload, "
+                         "the reference default is 2048")
     ap.add_argument("--rounds", type=int, default=100)
     ap.add_argument("--blocks-per-sm", type=int, default=8)
     ap.add_argument("--threads", type=int, default=256)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-peak", action="store_true")
+    ap.add_argument("--no-oldmalloc", action="store_true")
+    ap.add_argument("--pattern", default="warp", choices=["warp", "thread"],
+                    help="how each block is written and verified: by its warp, 512 B per instruction, or by its thread")
+    ap.add_argument("--oldmalloc-rounds", type=int, default=10, help="rounds of the CUDA device-malloc comparison")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target length of the CPU baseline sample")
+    ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--autotune", action="store_true", help="re-run the batched workload's autotuner first")
     return ap.parse_args()
 
 
@@ -196,6 +204,110 @@ def atomic_peak(torch, sms):
     return res
 
 
+def oldmalloc_column(torch, stream, heap_bytes, blocks, tpb, rounds, d_sizes, flush, pattern):
+    """The same stress on CUDA's built-in device malloc (the OldMalloc policy with
+    CudaSetLimits sizing its heap to the Scatter heap's size), over the first
+    `rounds` rows of the size table: the comparison column for the GB300 heap."""
+    from mallocmc_gb300 import _lib
+    from mallocmc_gb300.workloads import stress_params
+
+    L = _lib.lib()
+    _lib.check(L.mmc_oldmalloc_set_heap(heap_bytes, torch.cuda.current_device()), "oldmalloc heap")
+    stats = torch.zeros(4, dtype=torch.int64, device="cuda")
+    p = stress_params(blocks, tpb, rounds, 16, 1024, 16, SEED, pattern)
+    import ctypes
+
+    for _ in range(2):
+        _lib.check(L.mmc_run_stress_oldmalloc(ctypes.byref(p), d_sizes.data_ptr(), stats.data_ptr(),
+                                              stream.cuda_stream), "oldmalloc stress")
+    torch.cuda.synchronize()
+    stats.zero_()
+    ms = []
+    for _ in range(3):
+        flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        _lib.check(L.mmc_run_stress_oldmalloc(ctypes.byref(p), d_sizes.data_ptr(), stats.data_ptr(),
+                                              stream.cuda_stream), "oldmalloc stress")
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    st = stats.cpu().numpy().view(np.uint64)
+    pairs = blocks * tpb * rounds
+    return {"value": pairs / (statistics.median(ms) * 1e-3), "unit": UNIT, "policy": "OldMalloc+CudaSetLimits",
+            "rounds": rounds, "ms_per_launch": statistics.median(ms), "nulls": int(st[1]), "pattern_errors": int(st[2])}
+
+
+# The batched workload's geometry as chosen by mallocmc_gb300.autotune (coordinate
+# descent over pagesize, regionsize, hash primes, access block, grid) on a GB300.
+BATCH_TUNED = {"pagesize": 16384, "regionsize": 32, "hashingK": 65537, "hashingDistMP": 257,
+               "accessblock_fraction": 4, "blocks_per_sm": 8}
+
+
+def batched_column(torch, args, sms):
+    """512 uneven jobs on one 16 GiB heap: one persistent graph-captured launch
+    against one plain launch per job (same allocations, checked job by job)."""
+    from mallocmc_gb300 import AlignmentPolicies, Allocator, CreationPolicies, DistributionPolicies
+    from mallocmc_gb300.autotune import TuneConfig, _accessblock, autotune
+    from mallocmc_gb300.batch import Batch, expected_pairs, make_jobs
+
+    heap_bytes = 16 << 30
+    jobs = make_jobs(512, seed=3)
+    want = expected_pairs(jobs)
+    tune_trace = None
+    cfg = TuneConfig(**BATCH_TUNED)
+    if args.autotune:
+        cfg, _, tune_trace = autotune(jobs, heap_bytes, expected=want)
+
+    def run(cfg, label):
+        creation = CreationPolicies.Scatter(pagesize=cfg.pagesize, regionsize=cfg.regionsize,
+                                            accessblocksize=_accessblock(heap_bytes, cfg.pagesize,
+                                                                         cfg.accessblock_fraction),
+                                            hashingK=cfg.hashingK, hashingDistMP=cfg.hashingDistMP)
+        alloc = Allocator(creation, DistributionPolicies.XMallocSIMD(cfg.pagesize), None, None,
+                          AlignmentPolicies.Shrink(16), size=heap_bytes)
+        b = Batch(alloc, jobs, persistent_blocks=sms * cfg.blocks_per_sm, use_graph=True)
+        stream = torch.cuda.current_stream()
+        out = {}
+        for form, fn in (("plain", b.run_plain), ("graph", b.run)):
+            for _ in range(max(3, args.warmup)):
+                fn()
+            torch.cuda.synchronize()
+            b.stats(clear=True)
+            ms = []
+            for _ in range(args.steps):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                fn()
+                e1.record(stream)
+                torch.cuda.synchronize()
+                ms.append(e0.elapsed_time(e1))
+            st = b.stats(clear=True)
+            ok = (np.array_equal(st[:, 0].astype(np.int64), args.steps * want) and int(st[:, 1].sum()) == 0
+                  and int(st[:, 2].sum()) == 0)
+            if not ok:
+                raise RuntimeError(f"batched workload ({form}, {label}) failed its per-job check")
+            out[form] = statistics.median(ms)
+        b.close()
+        alloc.close()
+        return out
+
+    tuned = run(cfg, "tuned")
+    ref = run(TuneConfig(), "reference defaults")
+    pairs = int(want.sum())
+    res = {"workload": "512 jobs on a 16 GiB heap, threads log-uniform in [32, 65536], sizes geometric "
+                       "(mean 64 B, cap 4 KiB, padded to 16), 1-16 cycles per thread",
+           "pairs_per_step": pairs, "threads": int(sum(j.threads for j in jobs)),
+           "graph_value": pairs / (tuned["graph"] * 1e-3), "plain_value": pairs / (tuned["plain"] * 1e-3),
+           "speedup_graph_vs_plain": tuned["plain"] / tuned["graph"], "unit": UNIT,
+           "ms": tuned, "tuned_config": dict(cfg.__dict__),
+           "reference_defaults": {"ms": ref, "speedup_graph_vs_plain": ref["plain"] / ref["graph"],
+                                  "graph_value": pairs / (ref["graph"] * 1e-3)}}
+    if tune_trace is not None:
+        res["autotune_trace"] = tune_trace
+    return res
+
+
 def cpu_port_run(heap_gib, threads_total, rounds, target_s, workers):
     """The oracle port of the reference's CPU backend on `workers` host threads,
     on a bounded sample (virtual threads x rounds) of the same workload."""
@@ -296,7 +408,10 @@ def main():
     stats = torch.zeros(4, dtype=torch.int64, device="cuda")
     h_stats = torch.zeros(4, dtype=torch.int64).pin_memory()
     flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
-    params = stress_params(blocks, tpb, rounds, 16, 1024, 16, SEED, True)
+    from mallocmc_gb300.workloads import PATTERN_THREAD, PATTERN_WARP
+
+    pattern = PATTERN_WARP if args.pattern == "warp" else PATTERN_THREAD
+    params = stress_params(blocks, tpb, rounds, 16, 1024, 16, SEED, pattern)
 
     def step(sizes_ptr):
         launch_stress(alloc, params, sizes_ptr, stats.data_ptr(), stream)
@@ -379,6 +494,12 @@ def main():
         atomic = {"bound": "l2_atomic", "achieved": ach / 1e9, "peak": pk["atom_l2_32MiB"] / 1e9, "unit": "Gatomic/s",
                   "frac": ach / pk["atom_l2_32MiB"], "atomics_per_pair": work["atomics_per_pair"],
                   "peaks_measured_gops": {k: v / 1e9 for k, v in pk.items()}}
+    batched = None
+    if not args.no_batched:
+        batched = batched_column(torch, args, sms)
+    oldm = None
+    if not args.no_oldmalloc:
+        oldm = oldmalloc_column(torch, stream, heap_bytes, blocks, tpb, args.oldmalloc_rounds, d_sizes, flush, pattern)
     cpu = None
     if not args.no_cpu_baseline:
         workers = os.cpu_count() or 1
@@ -396,10 +517,13 @@ def main():
         "config": {"workload": f"uniform_stress_{args.heap_gib:g}GiB", "heap_bytes": heap_bytes,
                    "grid": f"{sms}x{args.blocks_per_sm} blocks x {tpb} threads", "rounds": rounds,
                    "sizes": "uniform {16,32,...,1024} (u16 table in HBM)",
+                   "pattern": (f"u64 pattern written and verified per block by its {args.pattern}"
+                               + (" (512 B per instruction)" if args.pattern == "warp" else " (16 B per store)")),
                    "policies": f"Scatter<4096,{args.accessblock_mib}MiB,16,2,noreset>+XMallocSIMD+ReturnNull+Shrink<16>",
                    "pairs_per_step": work["pairs"], "l2": "flushed between timed steps (512 MiB write)",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "roofline": roofline, "atomic_roofline": atomic, "cpu_baseline": cpu, "e2e": e2e,
+        "oldmalloc": oldm, "batched": batched,
         "gpu_launches": args.steps, "clocks": clk.summary(), "wall_s_timed": wall,
         "per_step_ms": ms,
     }

@@ -163,6 +163,17 @@ namespace mallocMC
                 return ss.str();
             }
         };
+        /* OldMalloc (creationPolicies/OldMalloc.hpp:46-84): CUDA's own device
+         * malloc/free; provides no slot count (:51). Pair it with
+         * ReservePoolPolicies::CudaSetLimits. */
+        class OldMalloc
+        {
+        public:
+            static constexpr bool providesAvailableSlots = false;
+            static constexpr bool usesHeap = false;
+            static void fill(mmc_config&) {}
+            static auto classname() -> std::string { return "OldMalloc"; }
+        };
     } // namespace CreationPolicies
 
     namespace DistributionPolicies
@@ -229,6 +240,13 @@ namespace mallocMC
         struct AlpakaBuf
         {
             static auto classname() -> std::string { return "AlpakaBuf"; }
+        };
+
+        /* CudaSetLimits (CudaSetLimits.hpp:57-78): sizes CUDA's device heap for
+         * OldMalloc through cudaLimitMallocHeapSize of the current context. */
+        struct CudaSetLimits
+        {
+            static auto classname() -> std::string { return "CudaSetLimits"; }
         };
     } // namespace ReservePoolPolicies
 
@@ -303,29 +321,45 @@ namespace mallocMC
         AllocatorHandleImpl() = default;
         explicit AllocatorHandleImpl(mmc_device_handle const& h) : devAllocator(h) {}
 
+        __device__ auto malloc(size_t size) -> void*
+        {
+            if constexpr(T_HostAllocator::CreationPolicy::usesHeap)
+                return mmc::dev::malloc<mmc::dev::GpuIds>(devAllocator, size);
+            else
+                return ::malloc(static_cast<size_t>(static_cast<uint32_t>(size))); /* OldMalloc.hpp:56-60 */
+        }
         template<typename AlpakaAcc>
         __device__ auto malloc(AlpakaAcc const&, size_t size) -> void*
         {
-            return mmc::dev::malloc<mmc::dev::GpuIds>(devAllocator, size);
+            return malloc(size);
         }
-        __device__ auto malloc(size_t size) -> void* { return mmc::dev::malloc<mmc::dev::GpuIds>(devAllocator, size); }
 
+        __device__ void free(void* p)
+        {
+            if constexpr(T_HostAllocator::CreationPolicy::usesHeap)
+                mmc::dev::free<mmc::dev::GpuIds>(devAllocator, p);
+            else
+                ::free(p); /* OldMalloc.hpp:62-66 */
+        }
         template<typename AlpakaAcc>
         __device__ void free(AlpakaAcc const&, void* p)
         {
-            mmc::dev::free<mmc::dev::GpuIds>(devAllocator, p);
+            free(p);
         }
-        __device__ void free(void* p) { mmc::dev::free<mmc::dev::GpuIds>(devAllocator, p); }
 
-        /* device_allocator.hpp:98-106; any subset of a warp's threads may call it */
+        /* device_allocator.hpp:98-106 (0 when the creation policy provides no
+         * count); any subset of a warp's threads may call it */
+        __device__ auto getAvailableSlots(size_t slotSize) -> unsigned
+        {
+            if constexpr(T_HostAllocator::CreationPolicy::providesAvailableSlots)
+                return mmc::dev::available_slots<mmc::dev::GpuIds>(devAllocator, slotSize);
+            else
+                return 0u;
+        }
         template<typename AlpakaAcc>
         __device__ auto getAvailableSlots(AlpakaAcc const&, size_t slotSize) -> unsigned
         {
-            return mmc::dev::available_slots<mmc::dev::GpuIds>(devAllocator, slotSize);
-        }
-        __device__ auto getAvailableSlots(size_t slotSize) -> unsigned
-        {
-            return mmc::dev::available_slots<mmc::dev::GpuIds>(devAllocator, slotSize);
+            return getAvailableSlots(slotSize);
         }
     };
 
@@ -368,11 +402,22 @@ namespace mallocMC
             alloc(queue, size);
         }
 
-        ~Allocator() { mmc_heap_destroy(heap_); }
+        ~Allocator()
+        {
+            if(heap_ != nullptr)
+                mmc_heap_destroy(heap_);
+            else
+                mmc_oldmalloc_set_heap(8192u, device_); /* CudaSetLimits::resetMemPool; fails after use, ignored */
+        }
 
         /* allocator.hpp:195-200 */
         void destructiveResize(int /*dev*/, cudaStream_t queue, size_t size)
         {
+            if(heap_ == nullptr)
+            {
+                detail::throw_status(mmc_oldmalloc_set_heap(size, device_), "destructiveResize");
+                return;
+            }
             detail::throw_status(mmc_heap_destructive_resize(heap_, size, queue), "destructiveResize");
             mmc_heap_device_handle(heap_, &handle_);
         }
@@ -396,16 +441,19 @@ namespace mallocMC
         /* allocator.hpp:227-233: pads, counts, waits */
         auto getAvailableSlots(int /*dev*/, cudaStream_t queue, size_t slotSize) -> unsigned
         {
+            if constexpr(!CreationPolicy::providesAvailableSlots)
+                return 0u; /* allocator.hpp:47-55 */
             unsigned out = 0;
             detail::throw_status(mmc_available_slots(heap_, slotSize, queue, &out), "getAvailableSlots");
             return out;
         }
 
-        /* allocator.hpp:235-241 */
+        /* allocator.hpp:235-241 (OldMalloc has no pool of its own: {nullptr, 0}) */
         auto getHeapLocations() -> HeapInfoVector
         {
             HeapInfo hi{};
-            mmc_heap_locations(heap_, &hi.p, &hi.size);
+            if(heap_ != nullptr)
+                mmc_heap_locations(heap_, &hi.p, &hi.size);
             return HeapInfoVector{hi};
         }
 
@@ -413,7 +461,8 @@ namespace mallocMC
         auto errorFlags(cudaStream_t queue = nullptr, bool clear = false) -> uint32_t
         {
             uint32_t f = 0;
-            detail::throw_status(mmc_heap_error(heap_, queue, &f, clear ? 1 : 0), "errorFlags");
+            if(heap_ != nullptr)
+                detail::throw_status(mmc_heap_error(heap_, queue, &f, clear ? 1 : 0), "errorFlags");
             return f;
         }
 
@@ -422,6 +471,13 @@ namespace mallocMC
     private:
         void alloc(cudaStream_t queue, size_t size)
         {
+            if constexpr(!CreationPolicy::usesHeap)
+            {
+                /* CudaSetLimits::setMemPool (CudaSetLimits.hpp:59-64); OldMalloc's
+                 * initHeap does nothing (OldMalloc.hpp:73-81) */
+                detail::throw_status(mmc_oldmalloc_set_heap(size, device_), "Allocator");
+                return;
+            }
             mmc_config c;
             mmc_config_default(&c);
             CreationPolicy::fill(c);

@@ -257,9 +257,12 @@ typedef struct mmc_stress_params
     uint32_t rounds;
     uint32_t lo, hi, step;
     uint64_t seed;
-    uint32_t write_pattern; /* 0: allocate/free only */
+    uint32_t write_pattern; /* MMC_PATTERN_THREAD or MMC_PATTERN_WARP: how each block is written and verified */
     uint32_t reserved;
 } mmc_stress_params;
+#define MMC_PATTERN_THREAD 1 /* each thread writes and verifies its own block, 16 bytes per store */
+#define MMC_PATTERN_WARP 2   /* the warp writes and verifies its lanes' blocks together, 512 bytes per
+                                instruction (threads_per_block must be a multiple of 32) */
 mmc_status mmc_run_stress(mmc_heap* heap, const mmc_stress_params* p, const uint16_t* sizes,
                           unsigned long long* stats, void* stream);
 
@@ -276,6 +279,53 @@ mmc_status mmc_run_alloc_offsets(mmc_heap* heap, uint32_t blocks, uint32_t threa
                                  uint32_t seed, int64_t* offsets, void* stream);
 mmc_status mmc_run_free_offsets(mmc_heap* heap, uint32_t blocks, uint32_t threads_per_block, const uint32_t* sizes,
                                 uint32_t seed, const int64_t* offsets, unsigned long long* errors, void* stream);
+
+/* ReservePoolPolicies::CudaSetLimits::setMemPool (reservePoolPolicies/CudaSetLimits.hpp:59-64):
+ * size CUDA's own device heap (cudaLimitMallocHeapSize of the current context)
+ * for CreationPolicies::OldMalloc. Must precede the first kernel that calls
+ * ::malloc in the process (CUDA refuses later changes). */
+mmc_status mmc_oldmalloc_set_heap(size_t bytes, int device);
+
+/* The uniform stress of mmc_run_stress with CreationPolicies::OldMalloc
+ * (creationPolicies/OldMalloc.hpp:46-84): ::malloc / ::free on CUDA's device
+ * heap, the comparison column for the Scatter heap. Same parameters and stats. */
+mmc_status mmc_run_stress_oldmalloc(const mmc_stress_params* p, const uint16_t* sizes, unsigned long long* stats,
+                                    void* stream);
+
+/* ------------------------------------------------------------ batches
+ * Many independent allocation jobs of uneven size on one heap. No counterpart
+ * in the reference (its callers launch one kernel per job); this is the
+ * batched, graph-captured launcher of uneven jobs. */
+
+/* One job: `threads` threads, each running a seeded number of cycles in
+ * [min_cycles, max_cycles] of {malloc(size), write a u64 pattern, verify, free};
+ * sizes geometric with mean `mean_size` bytes, capped at `max_size`, padded to 16. */
+typedef struct mmc_job
+{
+    uint32_t threads;
+    uint32_t item_begin; /* set by mmc_batch_create: first 256-thread work item */
+    uint64_t seed;
+    uint32_t mean_size;
+    uint32_t max_size;
+    uint32_t min_cycles;
+    uint32_t max_cycles;
+} mmc_job;
+
+typedef struct mmc_batch mmc_batch;
+
+/* Upload a job table (host array) for `heap`. persistent_blocks = 0 picks 8 x
+ * the SM count. use_graph != 0 captures {counter reset, persistent launch}
+ * into a CUDA graph that mmc_batch_run replays. */
+mmc_status mmc_batch_create(mmc_heap* heap, const mmc_job* jobs, uint32_t njobs, uint32_t persistent_blocks,
+                            int use_graph, void* stream, mmc_batch** out);
+/* Run the batch as one persistent launch (the captured graph if any). */
+mmc_status mmc_batch_run(mmc_batch* batch, void* stream);
+/* Run the same batch as one plain kernel launch per job. */
+mmc_status mmc_batch_run_plain(mmc_batch* batch, void* stream);
+/* Per-job counters {pairs, nulls, pattern errors, checksum} (njobs x 4) to host. */
+mmc_status mmc_batch_stats(mmc_batch* batch, void* stream, unsigned long long* out, int clear);
+mmc_status mmc_batch_info(const mmc_batch* batch, uint32_t* total_items, uint32_t* blocks, uint64_t* total_threads);
+mmc_status mmc_batch_destroy(mmc_batch* batch);
 
 /* Relaxed device-scope atomicOr throughput over `words` u32 words at `buf`
  * (device, zeroed by the caller): iters per thread, random word per op.

@@ -53,6 +53,11 @@ class MmcStressParams(ctypes.Structure):
     ]
 
 
+class MmcJob(ctypes.Structure):
+    _fields_ = [("threads", u32), ("item_begin", u32), ("seed", u64), ("mean_size", u32), ("max_size", u32),
+                ("min_cycles", u32), ("max_cycles", u32)]
+
+
 # name -> (restype, argtypes); every function declared in include/mallocmc_gb300.h
 SIGNATURES = {
     "mmc_config_default": (None, [ctypes.POINTER(MmcConfig)]),
@@ -79,6 +84,14 @@ SIGNATURES = {
     "mmc_run_verify": (ctypes.c_int, [vp, u32, u32, vp, u32, vp, vp, vp]),
     "mmc_run_alloc_offsets": (ctypes.c_int, [vp, u32, u32, vp, u32, vp, vp]),
     "mmc_run_free_offsets": (ctypes.c_int, [vp, u32, u32, vp, u32, vp, vp, vp]),
+    "mmc_oldmalloc_set_heap": (ctypes.c_int, [ctypes.c_size_t, ctypes.c_int]),
+    "mmc_run_stress_oldmalloc": (ctypes.c_int, [ctypes.POINTER(MmcStressParams), vp, vp, vp]),
+    "mmc_batch_create": (ctypes.c_int, [vp, ctypes.POINTER(MmcJob), u32, u32, ctypes.c_int, vp, ctypes.POINTER(vp)]),
+    "mmc_batch_run": (ctypes.c_int, [vp, vp]),
+    "mmc_batch_run_plain": (ctypes.c_int, [vp, vp]),
+    "mmc_batch_stats": (ctypes.c_int, [vp, vp, vp, ctypes.c_int]),
+    "mmc_batch_info": (ctypes.c_int, [vp, ctypes.POINTER(u32), ctypes.POINTER(u32), ctypes.POINTER(u64)]),
+    "mmc_batch_destroy": (ctypes.c_int, [vp]),
     "mmc_atomic_peak": (ctypes.c_int, [vp, u64, u32, u32, u32, ctypes.c_int, ctypes.c_int, vp, vp]),
 }
 

@@ -1,0 +1,124 @@
+"""Autotuner for the batched launcher: picks the heap geometry (pagesize,
+access block size, regionsize), the page-hash primes (hashingK, hashingDistMP)
+and the persistent grid size for a given job table.
+
+The search is coordinate descent: starting from the reference defaults, each
+parameter in turn is swept over its candidates with the others fixed, and the
+fastest value kept; two passes over all parameters. Every candidate is measured
+as the median of `repeats` CUDA-event-timed runs of the batch (one graph
+launch each) after one warm-up run, on a fresh heap. Candidates whose runs fail
+a job (a null allocation or a pattern error) are rejected.
+"""
+from __future__ import annotations
+
+import statistics
+from dataclasses import asdict, dataclass, replace
+
+import numpy as np
+
+# Candidate values. The hash primes are pairs (hashingK, hashingDistMP).
+PAGESIZES = (4096, 16384, 65536)
+REGIONSIZES = (8, 16, 32)
+HASH_PRIMES = ((38183, 17497), (7919, 101), (104729, 1009), (65537, 257))
+ACCESSBLOCK_FRACTIONS = (0, 4, 2, 1)  # heap / fraction, rounded down to whole MiB; 0: the default 2 GiB
+BLOCKS_PER_SM = (2, 4, 8, 16)
+
+
+@dataclass(frozen=True)
+class TuneConfig:
+    pagesize: int = 4096
+    regionsize: int = 16
+    hashingK: int = 38183
+    hashingDistMP: int = 17497
+    accessblock_fraction: int = 0
+    blocks_per_sm: int = 8
+
+
+def _accessblock(heap_bytes: int, pagesize: int, fraction: int) -> int:
+    """An access block that divides the page area into `fraction` blocks (the
+    page area is slightly smaller than the heap: metadata takes its share);
+    fraction 0 is the reference default of 2 GiB."""
+    if fraction == 0:
+        return 2 << 30
+    usable = heap_bytes - heap_bytes // (pagesize // 12 + 1) - (8 << 20)
+    ab = (usable // fraction) >> 20 << 20
+    return max(ab, pagesize * 64)
+
+
+def measure(cfg: TuneConfig, jobs, heap_bytes: int, device: int, sms: int, expected=None, repeats: int = 2):
+    """Median milliseconds of one batched (graph) run under cfg, or None if a job failed."""
+    import torch
+
+    from .allocator import Allocator
+    from .batch import Batch
+    from .policies import AlignmentPolicies, CreationPolicies, DistributionPolicies
+
+    creation = CreationPolicies.Scatter(pagesize=cfg.pagesize, regionsize=cfg.regionsize,
+                                        accessblocksize=_accessblock(heap_bytes, cfg.pagesize,
+                                                                     cfg.accessblock_fraction),
+                                        hashingK=cfg.hashingK, hashingDistMP=cfg.hashingDistMP)
+    alloc = Allocator(creation, DistributionPolicies.XMallocSIMD(cfg.pagesize), None, None,
+                      AlignmentPolicies.Shrink(16), size=heap_bytes, device=device)
+    batch = None
+    try:
+        batch = Batch(alloc, jobs, persistent_blocks=sms * cfg.blocks_per_sm, use_graph=True)
+        stream = torch.cuda.current_stream()
+        batch.run()
+        torch.cuda.synchronize()
+        batch.stats(clear=True)
+        times = []
+        for _ in range(repeats):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            batch.run()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            times.append(e0.elapsed_time(e1))
+        st = batch.stats(clear=True)
+        if int(st[:, 1].sum()) or int(st[:, 2].sum()):
+            return None
+        if expected is not None and not np.array_equal(st[:, 0].astype(np.int64), repeats * expected):
+            return None
+        return statistics.median(times)
+    finally:
+        if batch is not None:
+            batch.close()
+        alloc.close()
+
+
+def autotune(jobs, heap_bytes: int, device: int = 0, passes: int = 2, repeats: int = 2, expected=None,
+             log=None):
+    """Coordinate descent over TuneConfig; returns (best config, best ms, trace)."""
+    import torch
+
+    sms = torch.cuda.get_device_properties(device).multi_processor_count
+    space = {
+        "pagesize": PAGESIZES,
+        "regionsize": REGIONSIZES,
+        "hash": HASH_PRIMES,
+        "accessblock_fraction": ACCESSBLOCK_FRACTIONS,
+        "blocks_per_sm": BLOCKS_PER_SM,
+    }
+    best = TuneConfig()
+    cache = {}
+
+    def score(c):
+        if c not in cache:
+            cache[c] = measure(c, jobs, heap_bytes, device, sms, expected, repeats)
+            if log:
+                log(asdict(c), cache[c])
+        return cache[c]
+
+    best_ms = score(best)
+    for _ in range(passes):
+        for name, values in space.items():
+            for v in values:
+                if name == "hash":
+                    cand = replace(best, hashingK=v[0], hashingDistMP=v[1])
+                else:
+                    cand = replace(best, **{name: v})
+                ms = score(cand)
+                if ms is not None and (best_ms is None or ms < best_ms):
+                    best, best_ms = cand, ms
+    trace = [{"config": asdict(c), "ms": ms} for c, ms in cache.items()]
+    return best, best_ms, trace

@@ -22,7 +22,7 @@ LIB_NAME = "libmallocmc_gb300.so"
 LIB_PATH = os.path.join(PKG, LIB_NAME)
 EXAMPLES_PATH = os.path.join(PKG, "libmallocmc_examples.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["heap_capi.cu", "workloads.cu"]
+SOURCES = ["heap_capi.cu", "workloads.cu", "batch.cu"]
 EXAMPLE_SOURCES = ["cxx_examples.cu"]  # user-side code on the C++ API, linked against the library
 
 

@@ -1,0 +1,347 @@
+/* batch.cu — many independent allocation jobs on one heap, in one launch.
+ *
+ * A job is `threads` threads, each running `cycles` (drawn per thread in
+ * [min_cycles, max_cycles]) of {malloc(size), write a u64 pattern, verify it,
+ * free}; sizes are geometric with mean `mean_size` bytes, capped at `max_size`
+ * and padded to 16 (all draws seeded per job, thread and cycle, so every form
+ * of the launch performs the same allocations).
+ *
+ * Two forms of the same work:
+ *   plain       one kernel launch per job (grid = ceil(threads / 256))
+ *   persistent  one launch of a fixed grid whose blocks take work items
+ *               (256-thread slices of any job) from a device counter until the
+ *               batch is done; the counter reset and the launch are captured
+ *               once into a CUDA graph and replayed per run.
+ * Per-job counters {pairs, nulls, pattern errors, checksum} make the forms
+ * comparable job by job.
+ */
+#include "mmc_internal.h"
+
+#include <algorithm>
+#include <cmath>
+#include <new>
+#include <vector>
+
+using namespace mmc::host;
+namespace dv = mmc::dev;
+
+struct mmc_batch
+{
+    mmc_heap* heap;
+    mmc_device_handle handle;
+    int device;
+    uint32_t njobs;
+    uint32_t total_items;
+    uint32_t blocks;
+    uint32_t threads_per_block;
+    std::vector<mmc_job> host_jobs;
+    mmc_job* jobs;              /* device copy, item_begin filled */
+    unsigned* counter;          /* work-item counter of the persistent form */
+    unsigned long long* stats;  /* njobs x 4 */
+    cudaGraph_t graph;
+    cudaGraphExec_t exec;
+    cudaStream_t capture_stream;
+};
+
+namespace
+{
+    constexpr uint32_t kItemThreads = 256;
+
+    __host__ __device__ __forceinline__ uint64_t mix64(uint64_t seed, uint64_t a, uint64_t b)
+    {
+        uint64_t z = seed + a * 0x9E3779B97F4A7C15ull + b * 0xD1B54A32D192ED03ull;
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        return z ^ (z >> 31);
+    }
+
+    /* Size of cycle c of job thread jt: geometric on {1, 2, ...} with the job's
+     * mean (inverse-CDF draw), capped, padded to 16. */
+    __device__ __forceinline__ uint32_t draw_size(const mmc_job& j, uint64_t m)
+    {
+        const float u = (static_cast<float>(m >> 40) + 0.5f) * (1.0f / 16777216.0f); /* (0, 1) */
+        const float q = 1.0f - 1.0f / static_cast<float>(j.mean_size);
+        float x = 1.0f + floorf(logf(u) / logf(q));
+        if(!(x < static_cast<float>(j.max_size)))
+            x = static_cast<float>(j.max_size);
+        const uint32_t s = static_cast<uint32_t>(x);
+        return (s + 15u) & ~15u;
+    }
+
+    __device__ __forceinline__ void run_job_thread(const mmc_device_handle& h, const mmc_job& j, uint32_t jt,
+                                                   unsigned long long& pairs, unsigned long long& nulls,
+                                                   unsigned long long& bad, unsigned long long& csum)
+    {
+        const uint32_t span = j.max_cycles - j.min_cycles + 1u;
+        const uint32_t cycles = j.min_cycles + static_cast<uint32_t>(mix64(j.seed, jt, 0xC1C1Eull) >> 32) % span;
+        for(uint32_t c = 0; c < cycles; ++c)
+        {
+            const uint64_t m = mix64(j.seed, jt, c);
+            const uint32_t bytes = draw_size(j, m);
+            char* ptr = static_cast<char*>(dv::malloc<dv::GpuIds>(h, bytes));
+            if(ptr == nullptr)
+            {
+                ++nulls;
+                continue;
+            }
+            ulonglong2* q = reinterpret_cast<ulonglong2*>(ptr);
+            const uint32_t n16 = bytes / 16u;
+            for(uint32_t i = 0; i < n16; ++i)
+                q[i] = make_ulonglong2(m + 2u * i, m + 2u * i + 1u);
+            for(uint32_t i = 0; i < n16; ++i)
+            {
+                const ulonglong2 v = q[i];
+                bad += (v.x != m + 2u * i) + (v.y != m + 2u * i + 1u);
+                csum += v.x ^ v.y;
+            }
+            dv::free<dv::GpuIds>(h, ptr);
+            ++pairs;
+        }
+    }
+
+    __device__ __forceinline__ void flush_stats(unsigned long long* s, unsigned long long pairs,
+                                                unsigned long long nulls, unsigned long long bad,
+                                                unsigned long long csum)
+    {
+        /* every lane of the warp calls this (the kernels never exit lanes early) */
+        __syncwarp();
+        for(int off = 16; off > 0; off >>= 1)
+        {
+            pairs += __shfl_down_sync(0xFFFFFFFFu, pairs, off);
+            nulls += __shfl_down_sync(0xFFFFFFFFu, nulls, off);
+            bad += __shfl_down_sync(0xFFFFFFFFu, bad, off);
+            csum ^= __shfl_down_sync(0xFFFFFFFFu, csum, off);
+        }
+        if((threadIdx.x & 31u) == 0u)
+        {
+            if(pairs)
+                atomicAdd(&s[0], pairs);
+            if(nulls)
+                atomicAdd(&s[1], nulls);
+            if(bad)
+                atomicAdd(&s[2], bad);
+            if(csum)
+                atomicXor(&s[3], csum);
+        }
+    }
+} // namespace
+
+/* Plain form: one launch per job. */
+__global__ void __launch_bounds__(256) mmc_job_kernel(mmc_device_handle h, const mmc_job* jobs, uint32_t job,
+                                                      unsigned long long* stats)
+{
+    const mmc_job j = jobs[job];
+    const uint32_t jt = blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned long long pairs = 0, nulls = 0, bad = 0, csum = 0;
+    if(jt < j.threads)
+        run_job_thread(h, j, jt, pairs, nulls, bad, csum);
+    flush_stats(stats + 4ull * job, pairs, nulls, bad, csum);
+}
+
+/* Persistent form: blocks take 256-thread work items from *counter. */
+__global__ void __launch_bounds__(256) mmc_batch_kernel(mmc_device_handle h, const mmc_job* jobs, uint32_t njobs,
+                                                        uint32_t total_items, unsigned* counter,
+                                                        unsigned long long* stats)
+{
+    __shared__ uint32_t s_item, s_job;
+    for(;;)
+    {
+        if(threadIdx.x == 0)
+        {
+            const uint32_t item = atomicAdd(counter, 1u);
+            uint32_t lo = 0, hi = njobs; /* last job whose first item <= item */
+            if(item < total_items)
+                while(hi - lo > 1u)
+                {
+                    const uint32_t mid = (lo + hi) / 2u;
+                    if(jobs[mid].item_begin <= item)
+                        lo = mid;
+                    else
+                        hi = mid;
+                }
+            s_item = item;
+            s_job = lo;
+        }
+        __syncthreads();
+        const uint32_t item = s_item;
+        const uint32_t job = s_job;
+        __syncthreads();
+        if(item >= total_items)
+            return;
+        const mmc_job j = jobs[job];
+        const uint32_t jt = (item - j.item_begin) * kItemThreads + threadIdx.x;
+        unsigned long long pairs = 0, nulls = 0, bad = 0, csum = 0;
+        if(jt < j.threads)
+            run_job_thread(h, j, jt, pairs, nulls, bad, csum);
+        flush_stats(stats + 4ull * job, pairs, nulls, bad, csum);
+    }
+}
+
+namespace
+{
+    void release(mmc_batch* b)
+    {
+        if(b == nullptr)
+            return;
+        if(b->exec)
+            cudaGraphExecDestroy(b->exec);
+        if(b->graph)
+            cudaGraphDestroy(b->graph);
+        if(b->capture_stream)
+            cudaStreamDestroy(b->capture_stream);
+        if(b->jobs)
+            cudaFree(b->jobs);
+        if(b->counter)
+            cudaFree(b->counter);
+        if(b->stats)
+            cudaFree(b->stats);
+        delete b;
+    }
+
+    void launch_persistent(mmc_batch* b, cudaStream_t s)
+    {
+        cudaMemsetAsync(b->counter, 0, sizeof(unsigned), s);
+        mmc_batch_kernel<<<b->blocks, kItemThreads, 0, s>>>(b->handle, b->jobs, b->njobs, b->total_items, b->counter,
+                                                            b->stats);
+    }
+} // namespace
+
+extern "C" {
+
+mmc_status mmc_batch_create(mmc_heap* heap, const mmc_job* jobs, uint32_t njobs, uint32_t persistent_blocks,
+                            int use_graph, void* stream, mmc_batch** out)
+{
+    if(heap == nullptr || jobs == nullptr || out == nullptr || njobs == 0u)
+        return fail(MMC_ERR_ARG, "null argument or empty batch");
+    *out = nullptr;
+    mmc_batch* b = new(std::nothrow) mmc_batch();
+    if(b == nullptr)
+        return fail(MMC_ERR_OOM, "host allocation failed");
+    mmc_heap_device_handle(heap, &b->handle);
+    b->heap = heap;
+    cudaGetDevice(&b->device);
+    b->njobs = njobs;
+    b->threads_per_block = kItemThreads;
+    b->host_jobs.assign(jobs, jobs + njobs);
+    uint64_t items = 0;
+    for(auto& j : b->host_jobs)
+    {
+        if(j.threads == 0u || j.mean_size == 0u || j.max_size == 0u || j.min_cycles > j.max_cycles)
+        {
+            release(b);
+            return fail(MMC_ERR_ARG, "bad job descriptor");
+        }
+        j.item_begin = static_cast<uint32_t>(items);
+        items += (j.threads + kItemThreads - 1u) / kItemThreads;
+    }
+    if(items > 0xFFFFFFF0ull)
+    {
+        release(b);
+        return fail(MMC_ERR_ARG, "batch too large");
+    }
+    b->total_items = static_cast<uint32_t>(items);
+    b->blocks = persistent_blocks ? persistent_blocks : scan_grid(b->device) * 2u;
+    cudaStream_t s = as_stream(stream);
+    mmc_status st = cuda_check(cudaMalloc(&b->jobs, sizeof(mmc_job) * njobs), "cudaMalloc jobs");
+    if(st == MMC_OK)
+        st = cuda_check(cudaMalloc(&b->counter, sizeof(unsigned)), "cudaMalloc counter");
+    if(st == MMC_OK)
+        st = cuda_check(cudaMalloc(&b->stats, sizeof(unsigned long long) * 4ull * njobs), "cudaMalloc stats");
+    if(st == MMC_OK)
+        st = cuda_check(cudaMemcpyAsync(b->jobs, b->host_jobs.data(), sizeof(mmc_job) * njobs, cudaMemcpyHostToDevice, s),
+                        "copy jobs");
+    if(st == MMC_OK)
+        st = cuda_check(cudaMemsetAsync(b->stats, 0, sizeof(unsigned long long) * 4ull * njobs, s), "zero stats");
+    if(st == MMC_OK)
+        st = cuda_check(cudaStreamSynchronize(s), "wait for batch upload");
+    if(st == MMC_OK && use_graph)
+    {
+        st = cuda_check(cudaStreamCreateWithFlags(&b->capture_stream, cudaStreamNonBlocking), "capture stream");
+        if(st == MMC_OK)
+            st = cuda_check(cudaStreamBeginCapture(b->capture_stream, cudaStreamCaptureModeThreadLocal),
+                            "begin capture");
+        if(st == MMC_OK)
+        {
+            launch_persistent(b, b->capture_stream);
+            st = cuda_check(cudaStreamEndCapture(b->capture_stream, &b->graph), "end capture");
+        }
+        if(st == MMC_OK)
+            st = cuda_check(cudaGraphInstantiate(&b->exec, b->graph, 0), "instantiate graph");
+    }
+    if(st != MMC_OK)
+    {
+        release(b);
+        return st;
+    }
+    *out = b;
+    return MMC_OK;
+}
+
+mmc_status mmc_batch_run(mmc_batch* b, void* stream)
+{
+    if(b == nullptr)
+        return fail(MMC_ERR_ARG, "batch is null");
+    cudaStream_t s = as_stream(stream);
+    if(b->exec)
+        return cuda_check(cudaGraphLaunch(b->exec, s), "graph launch");
+    launch_persistent(b, s);
+    return cuda_check(cudaGetLastError(), "persistent batch kernel");
+}
+
+mmc_status mmc_batch_run_plain(mmc_batch* b, void* stream)
+{
+    if(b == nullptr)
+        return fail(MMC_ERR_ARG, "batch is null");
+    cudaStream_t s = as_stream(stream);
+    for(uint32_t i = 0; i < b->njobs; ++i)
+    {
+        const uint32_t grid = (b->host_jobs[i].threads + kItemThreads - 1u) / kItemThreads;
+        mmc_job_kernel<<<grid, kItemThreads, 0, s>>>(b->handle, b->jobs, i, b->stats);
+    }
+    return cuda_check(cudaGetLastError(), "plain job kernels");
+}
+
+mmc_status mmc_batch_stats(mmc_batch* b, void* stream, unsigned long long* out, int clear)
+{
+    if(b == nullptr || out == nullptr)
+        return fail(MMC_ERR_ARG, "null argument");
+    cudaStream_t s = as_stream(stream);
+    mmc_status st = cuda_check(cudaMemcpyAsync(out, b->stats, sizeof(unsigned long long) * 4ull * b->njobs,
+                                               cudaMemcpyDeviceToHost, s),
+                               "copy batch stats");
+    if(st == MMC_OK && clear)
+        st = cuda_check(cudaMemsetAsync(b->stats, 0, sizeof(unsigned long long) * 4ull * b->njobs, s), "clear stats");
+    if(st == MMC_OK)
+        st = cuda_check(cudaStreamSynchronize(s), "wait for batch stats");
+    return st;
+}
+
+mmc_status mmc_batch_info(const mmc_batch* b, uint32_t* total_items, uint32_t* blocks, uint64_t* total_threads)
+{
+    if(b == nullptr)
+        return fail(MMC_ERR_ARG, "batch is null");
+    if(total_items)
+        *total_items = b->total_items;
+    if(blocks)
+        *blocks = b->blocks;
+    if(total_threads)
+    {
+        uint64_t t = 0;
+        for(const auto& j : b->host_jobs)
+            t += j.threads;
+        *total_threads = t;
+    }
+    return MMC_OK;
+}
+
+mmc_status mmc_batch_destroy(mmc_batch* b)
+{
+    if(b == nullptr)
+        return MMC_OK;
+    cudaSetDevice(b->device);
+    cudaDeviceSynchronize();
+    release(b);
+    return MMC_OK;
+}
+
+} /* extern "C" */

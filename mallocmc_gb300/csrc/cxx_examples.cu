@@ -58,6 +58,36 @@ namespace
         mallocMC::ReservePoolPolicies::AlpakaBuf<Acc>,
         mallocMC::AlignmentPolicies::Shrink<>>;
 
+    using OldAllocator = mallocMC::Allocator<
+        Acc,
+        mallocMC::CreationPolicies::OldMalloc,
+        mallocMC::DistributionPolicies::Noop,
+        mallocMC::OOMPolicies::ReturnNull,
+        mallocMC::ReservePoolPolicies::CudaSetLimits,
+        mallocMC::AlignmentPolicies::Noop>;
+
+    __global__ void oldMallocKernel(OldAllocator::AllocatorHandle h, int length, unsigned long long* sums, int* fails)
+    {
+        const Acc acc{};
+        const unsigned id = blockIdx.x * blockDim.x + threadIdx.x;
+        int* a = static_cast<int*>(h.malloc(acc, length * sizeof(int)));
+        if(a == nullptr)
+        {
+            atomicAdd(fails, 1);
+            sums[id] = 0;
+            return;
+        }
+        unsigned long long s = 0;
+        for(int i = 0; i < length; ++i)
+            a[i] = static_cast<int>(id * length + i);
+        for(int i = 0; i < length; ++i)
+            s += static_cast<unsigned long long>(a[i]);
+        sums[id] = s;
+        if(h.getAvailableSlots(acc, 16) != 0u)
+            atomicAdd(fails, 1000); /* OldMalloc provides no count: must be 0 */
+        h.free(acc, a);
+    }
+
     __device__ int** arA;
     __device__ int** arB;
     __device__ int** arC;
@@ -229,6 +259,44 @@ int mmcx_bad_config(int device)
     catch(const std::invalid_argument&)
     {
         return 1;
+    }
+}
+
+/* The same policy API over CUDA's own device heap (CreationPolicies::OldMalloc
+ * with ReservePoolPolicies::CudaSetLimits): *sum over threads of their array
+ * sums, *gaussian the closed form n(n-1)/2, host slot count (0: no count). */
+int mmcx_oldmalloc(int device, int length, unsigned long long* sum, unsigned long long* gaussian, unsigned* slots,
+                   int* failures)
+{
+    try
+    {
+        cudaSetDevice(device);
+        OldAllocator alloc(device, nullptr, 64U * 1024U * 1024U);
+        const unsigned block = 64, grid = 8;
+        int* d_fail = nullptr;
+        unsigned long long* d_sums = nullptr;
+        cudaMalloc(&d_fail, sizeof(int));
+        cudaMemset(d_fail, 0, sizeof(int));
+        cudaMalloc(&d_sums, sizeof(unsigned long long) * block * grid);
+        oldMallocKernel<<<grid, block>>>(alloc.getAllocatorHandle(), length, d_sums, d_fail);
+        std::vector<unsigned long long> h(block * grid);
+        cudaMemcpy(h.data(), d_sums, sizeof(unsigned long long) * h.size(), cudaMemcpyDeviceToHost);
+        cudaMemcpy(failures, d_fail, sizeof(int), cudaMemcpyDeviceToHost);
+        unsigned long long s = 0;
+        for(auto v : h)
+            s += v;
+        *sum = s;
+        const unsigned long long n = static_cast<unsigned long long>(block) * grid * length;
+        *gaussian = n * (n - 1) / 2;
+        *slots = alloc.getAvailableSlots(device, nullptr, 16);
+        const cudaError_t e = cudaDeviceSynchronize();
+        cudaFree(d_fail);
+        cudaFree(d_sums);
+        return e == cudaSuccess ? 0 : 2;
+    }
+    catch(const std::exception& e)
+    {
+        return report(e);
     }
 }
 

@@ -54,6 +54,46 @@ __global__ void mmc_program_kernel(mmc_device_handle h, const uint8_t* kinds, co
 
 __global__ void mmc_store_result_kernel(const unsigned* src, int64_t* dst) { *dst = static_cast<int64_t>(*src); }
 
+/* Write then verify the u64 pattern m + i of `bytes` bytes at every lane's
+ * block, cooperatively: the warp walks the blocks of its lanes in turn and
+ * moves 512 contiguous bytes per instruction (16 per lane), instead of each
+ * lane streaming its own block 16 bytes at a time across 32 cache lines.
+ * Every lane of the warp must call it (blocks of lanes whose ptr is null are
+ * skipped). Returns the pattern mismatches found in this lane's share. */
+__device__ __forceinline__ unsigned long long warp_pattern(char* ptr, uint32_t bytes, uint64_t m,
+                                                           unsigned long long& csum)
+{
+    const uint32_t lane = threadIdx.x & 31u;
+    unsigned long long bad = 0;
+    const unsigned have = __ballot_sync(0xFFFFFFFFu, ptr != nullptr);
+    for(unsigned rest = have; rest != 0u; rest &= rest - 1u)
+    {
+        const int k = __ffs(static_cast<int>(rest)) - 1;
+        ulonglong2* q = reinterpret_cast<ulonglong2*>(__shfl_sync(0xFFFFFFFFu, reinterpret_cast<unsigned long long>(ptr), k));
+        const uint32_t n16 = __shfl_sync(0xFFFFFFFFu, bytes, k) / 16u;
+        const uint64_t mk = __shfl_sync(0xFFFFFFFFu, m, k);
+        for(uint32_t i = lane; i < n16; i += 32u)
+            q[i] = make_ulonglong2(mk + 2u * i, mk + 2u * i + 1u);
+    }
+    __syncwarp();
+    for(unsigned rest = have; rest != 0u; rest &= rest - 1u)
+    {
+        const int k = __ffs(static_cast<int>(rest)) - 1;
+        const ulonglong2* q
+            = reinterpret_cast<const ulonglong2*>(__shfl_sync(0xFFFFFFFFu, reinterpret_cast<unsigned long long>(ptr), k));
+        const uint32_t n16 = __shfl_sync(0xFFFFFFFFu, bytes, k) / 16u;
+        const uint64_t mk = __shfl_sync(0xFFFFFFFFu, m, k);
+        for(uint32_t i = lane; i < n16; i += 32u)
+        {
+            const ulonglong2 v = q[i];
+            bad += (v.x != mk + 2u * i) + (v.y != mk + 2u * i + 1u);
+            csum += v.x ^ v.y;
+        }
+    }
+    __syncwarp();
+    return bad;
+}
+
 /* Uniform stress: sizes[r * nthreads + t] or drawn from the seed. */
 __global__ void __launch_bounds__(256) mmc_stress_kernel(mmc_device_handle h, mmc_stress_params p,
                                                          const uint16_t* sizes, unsigned long long* stats)
@@ -68,12 +108,25 @@ __global__ void __launch_bounds__(256) mmc_stress_kernel(mmc_device_handle h, mm
         const uint32_t bytes
             = sizes ? sizes[r * nthreads + t] : p.lo + (static_cast<uint32_t>(m >> 32) % nsizes) * p.step;
         char* ptr = static_cast<char*>(dv::malloc<dv::GpuIds>(h, bytes));
+        if(p.write_pattern == MMC_PATTERN_WARP)
+        {
+            /* every lane takes part, with or without a block */
+            bad += warp_pattern(ptr, bytes, m, csum);
+            if(ptr == nullptr)
+                ++nulls;
+            else
+            {
+                dv::free<dv::GpuIds>(h, ptr);
+                ++pairs;
+            }
+            continue;
+        }
         if(ptr == nullptr)
         {
             ++nulls;
             continue;
         }
-        if(p.write_pattern)
+        if(p.write_pattern == MMC_PATTERN_THREAD)
         {
             /* 16-byte stores: chunks are 16-byte aligned under Shrink<16> */
             ulonglong2* q = reinterpret_cast<ulonglong2*>(ptr);
@@ -91,6 +144,71 @@ __global__ void __launch_bounds__(256) mmc_stress_kernel(mmc_device_handle h, mm
         ++pairs;
     }
     /* warp-aggregate the counters */
+    for(int off = 16; off > 0; off >>= 1)
+    {
+        pairs += __shfl_down_sync(0xFFFFFFFFu, pairs, off);
+        nulls += __shfl_down_sync(0xFFFFFFFFu, nulls, off);
+        bad += __shfl_down_sync(0xFFFFFFFFu, bad, off);
+        csum ^= __shfl_down_sync(0xFFFFFFFFu, csum, off);
+    }
+    if((threadIdx.x & 31u) == 0u)
+    {
+        atomicAdd(&stats[0], pairs);
+        if(nulls)
+            atomicAdd(&stats[1], nulls);
+        if(bad)
+            atomicAdd(&stats[2], bad);
+        atomicXor(&stats[3], csum);
+    }
+}
+
+/* The same stress on CUDA's device heap (CreationPolicies::OldMalloc, OldMalloc.hpp:59-68). */
+__global__ void __launch_bounds__(256) mmc_stress_oldmalloc_kernel(mmc_stress_params p, const uint16_t* sizes,
+                                                                   unsigned long long* stats)
+{
+    const uint64_t nthreads = static_cast<uint64_t>(gridDim.x) * blockDim.x;
+    const uint64_t t = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    const uint32_t nsizes = (p.hi - p.lo) / p.step + 1u;
+    unsigned long long pairs = 0, nulls = 0, bad = 0, csum = 0;
+    for(uint32_t r = 0; r < p.rounds; ++r)
+    {
+        const uint64_t m = mix64(p.seed, t, r);
+        const uint32_t bytes
+            = sizes ? sizes[r * nthreads + t] : p.lo + (static_cast<uint32_t>(m >> 32) % nsizes) * p.step;
+        char* ptr = static_cast<char*>(::malloc(bytes));
+        if(p.write_pattern == MMC_PATTERN_WARP)
+        {
+            bad += warp_pattern(ptr, bytes, m, csum);
+            if(ptr == nullptr)
+                ++nulls;
+            else
+            {
+                ::free(ptr);
+                ++pairs;
+            }
+            continue;
+        }
+        if(ptr == nullptr)
+        {
+            ++nulls;
+            continue;
+        }
+        if(p.write_pattern == MMC_PATTERN_THREAD)
+        {
+            ulonglong2* q = reinterpret_cast<ulonglong2*>(ptr);
+            const uint32_t n16 = bytes / 16u;
+            for(uint32_t i = 0; i < n16; ++i)
+                q[i] = make_ulonglong2(m + 2u * i, m + 2u * i + 1u);
+            for(uint32_t i = 0; i < n16; ++i)
+            {
+                const ulonglong2 v = q[i];
+                bad += (v.x != m + 2u * i) + (v.y != m + 2u * i + 1u);
+                csum += v.x ^ v.y;
+            }
+        }
+        ::free(ptr);
+        ++pairs;
+    }
     for(int off = 16; off > 0; off >>= 1)
     {
         pairs += __shfl_down_sync(0xFFFFFFFFu, pairs, off);
@@ -228,12 +346,37 @@ mmc_status mmc_run_stress(mmc_heap* heap, const mmc_stress_params* p, const uint
     if(heap == nullptr || p == nullptr || stats == nullptr)
         return fail(MMC_ERR_ARG, "null argument");
     if(p->blocks == 0u || p->threads_per_block == 0u || p->threads_per_block > 256u || p->step == 0u
-       || p->hi < p->lo)
+       || p->hi < p->lo || (p->write_pattern != MMC_PATTERN_THREAD && p->write_pattern != MMC_PATTERN_WARP)
+       || (p->write_pattern != MMC_PATTERN_THREAD && p->write_pattern != MMC_PATTERN_WARP)
+       || (p->write_pattern == MMC_PATTERN_WARP && (p->threads_per_block % 32u) != 0u))
         return fail(MMC_ERR_ARG, "bad stress parameters");
     mmc_device_handle h;
     mmc_heap_device_handle(heap, &h);
     mmc_stress_kernel<<<p->blocks, p->threads_per_block, 0, as_stream(stream)>>>(h, *p, sizes, stats);
     return cuda_check(cudaGetLastError(), "stress kernel");
+}
+
+mmc_status mmc_oldmalloc_set_heap(size_t bytes, int device)
+{
+    mmc_status st = cuda_check(cudaSetDevice(device), "cudaSetDevice");
+    if(st == MMC_OK)
+        st = cuda_check(cudaDeviceSetLimit(cudaLimitMallocHeapSize, bytes), "cudaDeviceSetLimit(MallocHeapSize)");
+    if(st != MMC_OK)
+        cudaGetLastError(); /* CUDA refuses the limit after ::malloc ran; do not leave the error pending
+                               (CudaSetLimits.hpp:66-72 clears it the same way) */
+    return st;
+}
+
+mmc_status mmc_run_stress_oldmalloc(const mmc_stress_params* p, const uint16_t* sizes, unsigned long long* stats,
+                                    void* stream)
+{
+    if(p == nullptr || stats == nullptr)
+        return fail(MMC_ERR_ARG, "null argument");
+    if(p->blocks == 0u || p->threads_per_block == 0u || p->threads_per_block > 256u || p->step == 0u
+       || p->hi < p->lo || (p->write_pattern == MMC_PATTERN_WARP && (p->threads_per_block % 32u) != 0u))
+        return fail(MMC_ERR_ARG, "bad stress parameters");
+    mmc_stress_oldmalloc_kernel<<<p->blocks, p->threads_per_block, 0, as_stream(stream)>>>(*p, sizes, stats);
+    return cuda_check(cudaGetLastError(), "OldMalloc stress kernel");
 }
 
 mmc_status mmc_run_verify(mmc_heap* heap, uint32_t blocks, uint32_t tpb, const uint32_t* sizes, uint32_t seed,

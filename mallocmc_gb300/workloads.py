@@ -51,7 +51,12 @@ def run_program(alloc: Allocator, ops, stream=None) -> np.ndarray:
     return out.cpu().numpy()
 
 
-def stress_params(blocks, threads_per_block, rounds, lo=16, hi=1024, step=16, seed=1, write_pattern=True):
+PATTERN_THREAD, PATTERN_WARP = 1, 2
+
+
+def stress_params(blocks, threads_per_block, rounds, lo=16, hi=1024, step=16, seed=1, write_pattern=PATTERN_THREAD):
+    """write_pattern: PATTERN_THREAD (each thread writes and verifies its own
+    block) or PATTERN_WARP (the warp does its lanes' blocks together, coalesced)."""
     p = L.MmcStressParams()
     p.blocks, p.threads_per_block, p.rounds = blocks, threads_per_block, rounds
     p.lo, p.hi, p.step, p.seed = lo, hi, step, seed
@@ -65,7 +70,7 @@ def launch_stress(alloc: Allocator, params, sizes_dev_ptr, stats_dev_ptr, stream
 
 
 def run_stress(alloc: Allocator, blocks, threads_per_block, rounds, lo=16, hi=1024, step=16, seed=1,
-               write_pattern=True, sizes=None, stream=None) -> dict:
+               write_pattern=PATTERN_THREAD, sizes=None, stream=None) -> dict:
     torch = _torch()
     dev = torch.device("cuda", alloc.device)
     stats = torch.zeros(4, dtype=torch.int64, device=dev)

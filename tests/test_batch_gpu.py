@@ -1,0 +1,53 @@
+"""Batched uneven jobs: one persistent, graph-captured launch against one
+plain launch per job. Every job's result (pairs, nulls, pattern errors and the
+XOR checksum of everything it read back) must be the same in both forms, i.e.
+the same alone and in the mix, and the pairs must equal the host's count of the
+cycle draws."""
+import numpy as np
+import pytest
+
+from oracle.oracle import HeapConfig
+from tests.test_parity_gpu import gpu_allocator
+from tests.test_verify_gpu import assert_all_free
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("use_graph", [True, False])
+def test_batch_matches_plain_launches(use_graph):
+    from mallocmc_gb300.batch import Batch, expected_pairs, make_jobs
+
+    jobs = make_jobs(njobs=48, seed=11, tmin=32, tmax=8192)
+    want = expected_pairs(jobs)
+    cfg = HeapConfig(4096, 256 << 20, 16, 2, False)
+    with gpu_allocator(cfg, 1 << 30) as alloc:
+        b = Batch(alloc, jobs, persistent_blocks=0, use_graph=use_graph)
+        b.run_plain()
+        plain = b.stats()
+        b.run()
+        b.run()
+        batched = b.stats()
+        b.close()
+        assert np.array_equal(plain[:, 0].astype(np.int64), want)
+        assert int(plain[:, 1].sum()) == 0 and int(plain[:, 2].sum()) == 0
+        assert np.array_equal(batched[:, 0].astype(np.int64), 2 * want)
+        assert int(batched[:, 1].sum()) == 0 and int(batched[:, 2].sum()) == 0
+        # two runs XOR their (identical) checksums away; one plain run keeps it
+        assert int(batched[:, 3].astype(np.uint64).max()) == 0
+        assert_all_free(alloc.snapshot())
+        assert alloc.error_flags() == 0
+
+
+def test_batch_checksums_equal_across_forms():
+    from mallocmc_gb300.batch import Batch, make_jobs
+
+    jobs = make_jobs(njobs=32, seed=12, tmin=32, tmax=4096)
+    cfg = HeapConfig(16384, 256 << 20, 8, 2, False)
+    with gpu_allocator(cfg, 1 << 30) as alloc:
+        b = Batch(alloc, jobs, persistent_blocks=152 * 2, use_graph=True)
+        b.run_plain()
+        plain = b.stats()
+        b.run()
+        batched = b.stats()
+        b.close()
+        assert np.array_equal(plain, batched)

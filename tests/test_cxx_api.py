@@ -22,6 +22,9 @@ def ex():
                                  ctypes.POINTER(ctypes.c_int)]
     L.mmcx_example03.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint)]
     L.mmcx_bad_config.argtypes = [ctypes.c_int]
+    L.mmcx_oldmalloc.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_ulonglong),
+                                 ctypes.POINTER(ctypes.c_ulonglong), ctypes.POINTER(ctypes.c_uint),
+                                 ctypes.POINTER(ctypes.c_int)]
     L.mmcx_info.argtypes = [ctypes.c_char_p, ctypes.c_size_t]
     return L
 
@@ -62,3 +65,14 @@ def test_example03_device_side_slots(ex):
     fresh = OracleHeap(HeapConfig(4096, 256 << 20, 16, 2, False), 1 << 30).available_slots(1)
     assert np.all(slots == fresh - 254)
     assert host.value == fresh - 254
+
+
+@pytest.mark.gpu
+def test_oldmalloc_policy_on_cuda_device_heap(ex):
+    """CreationPolicies::OldMalloc + ReservePoolPolicies::CudaSetLimits: the same
+    handle API on CUDA's own device heap; no slot count (OldMalloc.hpp:51)."""
+    s, g, slots, fails = ctypes.c_ulonglong(), ctypes.c_ulonglong(), ctypes.c_uint(), ctypes.c_int()
+    assert ex.mmcx_oldmalloc(0, 50, ctypes.byref(s), ctypes.byref(g), ctypes.byref(slots), ctypes.byref(fails)) == 0
+    assert fails.value == 0
+    assert s.value == g.value
+    assert slots.value == 0

@@ -188,6 +188,23 @@ def test_page_based_allocations_concurrent():
         assert alloc.error_flags() == 0
 
 
+def test_stress_warp_pattern_mode():
+    """The warp-cooperative pattern mode writes and verifies every lane's whole
+    block (512 bytes per instruction); counts and cleanliness as in the per-thread mode."""
+    import torch
+
+    from mallocmc_gb300.workloads import PATTERN_WARP, run_stress
+
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    cfg = HeapConfig(4096, 256 << 20, 16, 2, False)
+    with gpu_allocator(cfg, 1 << 30) as alloc:
+        st = run_stress(alloc, sms * 4, 256, 20, 16, 1024, 16, seed=9, write_pattern=PATTERN_WARP)
+        assert st["pairs"] == sms * 4 * 256 * 20
+        assert st["nulls"] == 0 and st["bad"] == 0
+        assert_all_free(alloc.snapshot())
+        assert alloc.error_flags() == 0
+
+
 def test_stress_full_size_steps_no_corruption():
     """The benchmark workload (8 GiB heap, SMs x 8 x 256 threads, 100 rounds of
     malloc / u64 pattern / verify / free) three times back to back: no block may
