@@ -61,6 +61,8 @@ def parse():
     ap.add_argument("--oldmalloc-rounds", type=int, default=10, help="rounds of the CUDA device-malloc comparison")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target length of the CPU baseline sample")
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--serve-seconds", type=float, default=1.0, help="arrival window per rate of the serving loop")
     ap.add_argument("--autotune", action="store_true", help="re-run the batched workload's autotuner first")
     return ap.parse_args()
 
@@ -240,8 +242,8 @@ def oldmalloc_column(torch, stream, heap_bytes, blocks, tpb, rounds, d_sizes, fl
 
 # The batched workload's geometry as chosen by mallocmc_gb300.autotune (coordinate
 # descent over pagesize, regionsize, hash primes, access block, grid) on a GB300.
-BATCH_TUNED = {"pagesize": 16384, "regionsize": 32, "hashingK": 65537, "hashingDistMP": 257,
-               "accessblock_fraction": 4, "blocks_per_sm": 8}
+BATCH_TUNED = {"pagesize": 16384, "regionsize": 32, "hashingK": 7919, "hashingDistMP": 101,
+               "accessblock_fraction": 1, "blocks_per_sm": 8}
 
 
 def batched_column(torch, args, sms):
@@ -306,6 +308,47 @@ def batched_column(torch, args, sms):
     if tune_trace is not None:
         res["autotune_trace"] = tune_trace
     return res
+
+
+def serving_column(torch, args):
+    """Continuous batching on a 64 GiB device-resident heap (pagesize 64 KiB, so a
+    16 KiB chunk is a plain chunk): Poisson arrivals at each rate, lognormal
+    lengths (median 1024, sigma 1, cap 32768 elements of 2 B), one 16 KiB chunk per
+    256 elements, admission by the free-chunk count; one graph launch per tick
+    against one launch per live request per tick. Latency = admit to completion."""
+    from mallocmc_gb300 import AlignmentPolicies, Allocator, CreationPolicies, DistributionPolicies
+    from mallocmc_gb300.serve import Server, expected_checksum, make_requests
+
+    heap_bytes = 64 << 30
+    creation = CreationPolicies.Scatter(pagesize=65536, accessblocksize=16 << 30, regionsize=16)
+    alloc = Allocator(creation, DistributionPolicies.XMallocSIMD(65536), None, None, AlignmentPolicies.Shrink(16),
+                      size=heap_bytes)
+    srv = Server(alloc, slots=4096, max_chunks=128, step=64, queue_cap=8192)
+    rows = []
+    for rate in (1000, 10000, 100000):
+        n = int(min(rate * args.serve_seconds, 50000))
+        arrivals, lengths, seeds = make_requests(n, rate, seed=rate)
+        want = np.array([expected_checksum(int(s), int(l)) for s, l in zip(seeds, lengths)], dtype=np.uint64)
+        for mode in ("graph_per_tick", "launch_per_request"):
+            res = srv.run(arrivals, lengths, seeds, batched=(mode == "graph_per_tick"), realtime=True,
+                          max_seconds=max(5.0, 4 * args.serve_seconds))
+            ok = ~np.isnan(res["done"])
+            lat = (res["done"] - res["admit"])[ok] * 1e3
+            qlat = (res["done"] - arrivals)[ok] * 1e3
+            span = float(np.nanmax(res["done"]) - arrivals[0]) if ok.any() else float("nan")
+            rows.append({"rate_per_s": rate, "mode": mode, "requests": n, "completed": int(ok.sum()),
+                         "checksum_errors": int((res["checksum"][ok] != want[ok]).sum()),
+                         "p50_ms": float(np.percentile(lat, 50)) if ok.any() else None,
+                         "p99_ms": float(np.percentile(lat, 99)) if ok.any() else None,
+                         "p99_arrival_to_done_ms": float(np.percentile(qlat, 99)) if ok.any() else None,
+                         "throughput_req_per_s": ok.sum() / span if ok.any() else 0.0,
+                         "chunks_per_s": float((-(-lengths[ok] // 256)).sum() / span) if ok.any() else 0.0,
+                         "ticks": res["ticks"]})
+    srv.close()
+    alloc.close()
+    return {"workload": "64 GiB heap, pagesize 64 KiB; Poisson arrivals; lognormal lengths (median 1024, sigma 1, "
+                        "cap 32768) of 2-byte elements; a 16 KiB chunk per 256 elements; 64 elements per tick",
+            "latency": "admit to completion (host clock at the admitting and completing ticks)", "rows": rows}
 
 
 def cpu_port_run(heap_gib, threads_total, rounds, target_s, workers):
@@ -497,6 +540,9 @@ def main():
     batched = None
     if not args.no_batched:
         batched = batched_column(torch, args, sms)
+    serving = None
+    if not args.no_serve:
+        serving = serving_column(torch, args)
     oldm = None
     if not args.no_oldmalloc:
         oldm = oldmalloc_column(torch, stream, heap_bytes, blocks, tpb, args.oldmalloc_rounds, d_sizes, flush, pattern)
@@ -523,7 +569,7 @@ def main():
                    "pairs_per_step": work["pairs"], "l2": "flushed between timed steps (512 MiB write)",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "roofline": roofline, "atomic_roofline": atomic, "cpu_baseline": cpu, "e2e": e2e,
-        "oldmalloc": oldm, "batched": batched,
+        "oldmalloc": oldm, "batched": batched, "serving": serving,
         "gpu_launches": args.steps, "clocks": clk.summary(), "wall_s_timed": wall,
         "per_step_ms": ms,
     }

@@ -585,7 +585,8 @@ namespace mmc
             return nullptr;
         }
 
-        /* allocPageBasedSingle, Scatter.hpp:824-840, with a bounded, backed-off mutex wait. */
+        /* allocPageBasedSingle, Scatter.hpp:824-840, with a bounded, backed-off
+         * mutex wait: the reference's serial protocol, used for SerialIds. */
         __device__ inline void* alloc_page_based_single(const mmc_device_handle& h, u32 bytes)
         {
             u32 ns = 32u;
@@ -610,19 +611,83 @@ namespace mmc
             return res;
         }
 
-        /* allocPageBased, Scatter.hpp:848-866: the active lanes of a warp take turns. */
+        /* allocPageBasedSingleRegion's search (Scatter.hpp:775-813) for concurrent
+         * callers, without the global mutex. The chunk-size words are read 16 pages
+         * at a time (independent loads issued together, not one round trip per
+         * page), free runs are counted exactly as the reference counts them
+         * (downward, reset at a used page), and markpages' CAS decides who owns a
+         * run. A lane that loses a run to a concurrent claim starts counting again
+         * below it. With no concurrent caller this finds the reference's run and
+         * updates the hint as the reference does. */
+        __device__ inline void* alloc_page_based_scan(const mmc_device_handle& h, u32 startpage, u32 endpage,
+                                                      u32 bytes)
+        {
+            const u32 pagestoalloc = divup(bytes, h.pagesize);
+            u32 freecount = 0;
+            bool left_free = false;
+            /* the reference visits startpage down to endpage, both included
+             * (Scatter.hpp:785-787); pages top-1, top-2, ..., endpage remain */
+            u32 top = startpage + 1u;
+            while(top > endpage)
+            {
+                const u32 lo = (top - endpage > 16u) ? top - 16u : endpage;
+                u32 v[16];
+#pragma unroll
+                for(u32 k = 0; k < 16u; ++k)
+                {
+                    const u32 q = top - 1u - k;
+                    v[k] = (q >= lo && q < h.numpages) ? __ldcg(&h.chunksize[q]) : 1u;
+                }
+#pragma unroll
+                for(u32 k = 0; k < 16u; ++k)
+                {
+                    const u32 q = top - 1u - k;
+                    if(q < lo)
+                        break;
+                    if(v[k] == 0u)
+                    {
+                        if(++freecount == pagestoalloc)
+                        {
+                            if(q + pagestoalloc <= h.numpages && markpages(h, q, pagestoalloc, bytes))
+                            {
+                                if(!left_free)
+                                {
+                                    u32 nf = q - 1u;
+                                    if(!h.reference_quirks && q == 0u)
+                                        nf = 0u;
+                                    atomicCAS(&h.state->firstFreePageBased, startpage, nf);
+                                }
+                                return page_data(h, q);
+                            }
+                            freecount = 0u;
+                            left_free = true;
+                        }
+                    }
+                    else
+                    {
+                        left_free = true;
+                        freecount = 0u;
+                    }
+                }
+                top = lo;
+            }
+            return nullptr;
+        }
+
+        /* allocPageBased, Scatter.hpp:848-866. Alone on the heap (SerialIds) this
+         * is the reference's mutex-serialised search. With real thread ids every
+         * lane searches at once, lock-free (alloc_page_based_scan): the mutex
+         * serialised every large request in the GPU, and each search walks the
+         * page table one round trip per page. */
         template<class Ids>
         __device__ void* alloc_page_based(const mmc_device_handle& h, u32 bytes)
         {
             if(Ids::warpSize == 1u)
                 return alloc_page_based_single(h, bytes);
-            void* res = nullptr;
-            const u32 mask = __activemask();
-            const u32 num = static_cast<u32>(__popc(mask));
-            const u32 local_id = static_cast<u32>(__popc(lanemask_lt() & mask));
-            for(u32 active = 0; active < num; ++active)
-                if(active == local_id)
-                    res = alloc_page_based_single(h, bytes);
+            const u32 spage = ld_rlx(&h.state->firstFreePageBased);
+            void* res = alloc_page_based_scan(h, spage, 0u, bytes);
+            if(res == nullptr)
+                res = alloc_page_based_scan(h, h.numpages, spage, bytes);
             return res;
         }
 

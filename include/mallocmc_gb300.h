@@ -292,6 +292,40 @@ mmc_status mmc_oldmalloc_set_heap(size_t bytes, int device);
 mmc_status mmc_run_stress_oldmalloc(const mmc_stress_params* p, const uint16_t* sizes, unsigned long long* stats,
                                     void* stream);
 
+/* ------------------------------------------------------- fragmentation
+ * Fill until the first NULL, free a chosen half, refill: the heap's fill
+ * fraction at out-of-memory under a mix of small and multi-page requests.
+ * Request i of a phase has the size oracle/scatter_oracle.h's oc_frag_size
+ * describes (with probability large_permille/1000 log-uniform in
+ * [large_lo, large_hi], else uniform in [small_lo, small_hi]); thread t takes
+ * requests first_request + t, + T, + 2T, ... (T threads). */
+typedef struct mmc_frag_params
+{
+    uint32_t blocks;
+    uint32_t threads_per_block;
+    uint64_t seed;
+    uint64_t first_request;
+    uint32_t small_lo, small_hi;
+    uint32_t large_lo, large_hi;
+    uint32_t large_permille;
+    uint32_t max_per_thread; /* bound on one thread's requests in a phase */
+} mmc_frag_params;
+
+/* Allocate until the first NULL anywhere (a device flag stops every thread
+ * before its next request). Each block gets a u64 tag every 4 KiB and at its
+ * end, and is appended to the list ptrs/sizes (capacity entries; counters[0]
+ * is the list length, counters[1] the live requested bytes, counters[2] the
+ * requests made, counters[3] tag errors, counters[4] the stop flag, which the
+ * caller zeroes before a phase). */
+mmc_status mmc_run_fill(mmc_heap* heap, const mmc_frag_params* p, void** ptrs, uint32_t* sizes, uint64_t capacity,
+                        unsigned long long* counters, void* stream);
+/* Free the list entries idx[0..n) after checking their tags (counters as above). */
+mmc_status mmc_run_free_list(mmc_heap* heap, void** ptrs, uint32_t* sizes, const uint32_t* idx, uint64_t n,
+                             unsigned long long* counters, void* stream);
+/* Check the tags of every live entry of the list (counters[3] += errors). */
+mmc_status mmc_run_verify_list(mmc_heap* heap, void* const* ptrs, const uint32_t* sizes, uint64_t n,
+                               unsigned long long* counters, void* stream);
+
 /* ------------------------------------------------------------ batches
  * Many independent allocation jobs of uneven size on one heap. No counterpart
  * in the reference (its callers launch one kernel per job); this is the
@@ -326,6 +360,56 @@ mmc_status mmc_batch_run_plain(mmc_batch* batch, void* stream);
 mmc_status mmc_batch_stats(mmc_batch* batch, void* stream, unsigned long long* out, int clear);
 mmc_status mmc_batch_info(const mmc_batch* batch, uint32_t* total_items, uint32_t* blocks, uint64_t* total_threads);
 mmc_status mmc_batch_destroy(mmc_batch* batch);
+
+/* ------------------------------------------------------------ serving
+ * A continuous-batching request server on the device-resident heap. No
+ * counterpart in the reference. A request grows to final_len 2-byte elements,
+ * holding one 16 KiB chunk per 256 elements, and completes by checksumming its
+ * elements (sum of value x (index + 1), values a seeded function of seed and
+ * index) and freeing its chunks. */
+#define MMC_SERVE_FREE 0u
+#define MMC_SERVE_LIVE 1u
+#define MMC_SERVE_DONE 2u
+
+typedef struct mmc_serve_slot
+{
+    uint32_t id;
+    uint32_t final_len;
+    uint32_t len;     /* elements written so far */
+    uint32_t nchunks; /* chunks held */
+    uint64_t seed;
+    uint32_t state;   /* MMC_SERVE_* */
+    uint32_t failed;  /* ticks whose chunk allocation failed (retried) */
+    uint64_t checksum;
+} mmc_serve_slot;
+
+/* One command for the next tick: kind 1 admits request `id` into `slot`;
+ * kind 2 releases a completed slot. */
+typedef struct mmc_serve_cmd
+{
+    uint32_t kind;
+    uint32_t slot;
+    uint32_t id;
+    uint32_t final_len;
+    uint64_t seed;
+} mmc_serve_cmd;
+
+typedef struct mmc_server mmc_server;
+
+/* A server for `slots` concurrent requests of at most max_chunks chunks that
+ * grow `step` elements per tick; at most queue_cap commands per tick. The
+ * batched tick is captured into a CUDA graph here. */
+mmc_status mmc_serve_create(mmc_heap* heap, uint32_t slots, uint32_t max_chunks, uint32_t step, uint32_t queue_cap,
+                            mmc_server** out);
+/* Pinned host views: the command queue and its length (written by the host
+ * before a tick), the slot table and the free 16 KiB chunk count (as of the
+ * end of the last tick). */
+mmc_status mmc_serve_queue(mmc_server* server, mmc_serve_cmd** queue, uint32_t** queue_len, mmc_serve_slot** slots,
+                           unsigned** free_chunks);
+/* Run one tick and wait for it: batched != 0 replays the captured graph (all
+ * live requests in one launch); 0 launches one kernel per live request. */
+mmc_status mmc_serve_tick(mmc_server* server, int batched);
+mmc_status mmc_serve_destroy(mmc_server* server);
 
 /* Relaxed device-scope atomicOr throughput over `words` u32 words at `buf`
  * (device, zeroed by the caller): iters per thread, random word per op.

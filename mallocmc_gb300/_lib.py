@@ -15,6 +15,7 @@ MMC_OK, MMC_ERR_CONFIG, MMC_ERR_CUDA, MMC_ERR_TIMEOUT, MMC_ERR_OOM, MMC_ERR_ARG 
 MMC_DIST_NOOP, MMC_DIST_XMALLOCSIMD = 0, 1
 MMC_OOM_RETURNNULL, MMC_OOM_FLAG = 0, 1
 MMC_DEVERR_TIMEOUT, MMC_DEVERR_BADFREE, MMC_DEVERR_OOM = 0x1, 0x2, 0x4
+MMC_SERVE_FREE, MMC_SERVE_LIVE, MMC_SERVE_DONE = 0, 1, 2
 
 u32, u64, i64, vp = ctypes.c_uint32, ctypes.c_uint64, ctypes.c_int64, ctypes.c_void_p
 
@@ -58,6 +59,21 @@ class MmcJob(ctypes.Structure):
                 ("min_cycles", u32), ("max_cycles", u32)]
 
 
+class MmcServeSlot(ctypes.Structure):
+    _fields_ = [("id", u32), ("final_len", u32), ("len", u32), ("nchunks", u32), ("seed", u64), ("state", u32),
+                ("failed", u32), ("checksum", u64)]
+
+
+class MmcServeCmd(ctypes.Structure):
+    _fields_ = [("kind", u32), ("slot", u32), ("id", u32), ("final_len", u32), ("seed", u64)]
+
+
+class MmcFragParams(ctypes.Structure):
+    _fields_ = [("blocks", u32), ("threads_per_block", u32), ("seed", u64), ("first_request", u64),
+                ("small_lo", u32), ("small_hi", u32), ("large_lo", u32), ("large_hi", u32),
+                ("large_permille", u32), ("max_per_thread", u32)]
+
+
 # name -> (restype, argtypes); every function declared in include/mallocmc_gb300.h
 SIGNATURES = {
     "mmc_config_default": (None, [ctypes.POINTER(MmcConfig)]),
@@ -92,6 +108,14 @@ SIGNATURES = {
     "mmc_batch_stats": (ctypes.c_int, [vp, vp, vp, ctypes.c_int]),
     "mmc_batch_info": (ctypes.c_int, [vp, ctypes.POINTER(u32), ctypes.POINTER(u32), ctypes.POINTER(u64)]),
     "mmc_batch_destroy": (ctypes.c_int, [vp]),
+    "mmc_serve_create": (ctypes.c_int, [vp, u32, u32, u32, u32, ctypes.POINTER(vp)]),
+    "mmc_serve_queue": (ctypes.c_int, [vp, ctypes.POINTER(vp), ctypes.POINTER(vp), ctypes.POINTER(vp),
+                                       ctypes.POINTER(vp)]),
+    "mmc_serve_tick": (ctypes.c_int, [vp, ctypes.c_int]),
+    "mmc_serve_destroy": (ctypes.c_int, [vp]),
+    "mmc_run_fill": (ctypes.c_int, [vp, ctypes.POINTER(MmcFragParams), vp, vp, u64, vp, vp]),
+    "mmc_run_free_list": (ctypes.c_int, [vp, vp, vp, vp, u64, vp, vp]),
+    "mmc_run_verify_list": (ctypes.c_int, [vp, vp, vp, u64, vp, vp]),
     "mmc_atomic_peak": (ctypes.c_int, [vp, u64, u32, u32, u32, ctypes.c_int, ctypes.c_int, vp, vp]),
 }
 

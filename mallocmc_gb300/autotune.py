@@ -5,8 +5,9 @@ and the persistent grid size for a given job table.
 The search is coordinate descent: starting from the reference defaults, each
 parameter in turn is swept over its candidates with the others fixed, and the
 fastest value kept; two passes over all parameters. Every candidate is measured
-as the median of `repeats` CUDA-event-timed runs of the batch (one graph
-launch each) after one warm-up run, on a fresh heap. Candidates whose runs fail
+on a fresh heap as the median of `repeats` CUDA-event-timed runs of the batch
+(one graph launch each) after three warm-up runs, so geometries that degrade
+as the heap ages are judged aged. Candidates whose runs fail
 a job (a null allocation or a pattern error) are rejected.
 """
 from __future__ import annotations
@@ -45,8 +46,11 @@ def _accessblock(heap_bytes: int, pagesize: int, fraction: int) -> int:
     return max(ab, pagesize * 64)
 
 
-def measure(cfg: TuneConfig, jobs, heap_bytes: int, device: int, sms: int, expected=None, repeats: int = 2):
-    """Median milliseconds of one batched (graph) run under cfg, or None if a job failed."""
+def measure(cfg: TuneConfig, jobs, heap_bytes: int, device: int, sms: int, expected=None, repeats: int = 3,
+            warmups: int = 3):
+    """Median milliseconds of one batched (graph) run under cfg once the heap has
+    aged (after `warmups` runs: some geometries degrade as pages keep their
+    chunk formats and region counters fill), or None if a job failed."""
     import torch
 
     from .allocator import Allocator
@@ -63,7 +67,8 @@ def measure(cfg: TuneConfig, jobs, heap_bytes: int, device: int, sms: int, expec
     try:
         batch = Batch(alloc, jobs, persistent_blocks=sms * cfg.blocks_per_sm, use_graph=True)
         stream = torch.cuda.current_stream()
-        batch.run()
+        for _ in range(warmups):
+            batch.run()
         torch.cuda.synchronize()
         batch.stats(clear=True)
         times = []
@@ -86,7 +91,7 @@ def measure(cfg: TuneConfig, jobs, heap_bytes: int, device: int, sms: int, expec
         alloc.close()
 
 
-def autotune(jobs, heap_bytes: int, device: int = 0, passes: int = 2, repeats: int = 2, expected=None,
+def autotune(jobs, heap_bytes: int, device: int = 0, passes: int = 2, repeats: int = 3, expected=None,
              log=None):
     """Coordinate descent over TuneConfig; returns (best config, best ms, trace)."""
     import torch

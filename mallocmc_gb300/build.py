@@ -22,8 +22,9 @@ LIB_NAME = "libmallocmc_gb300.so"
 LIB_PATH = os.path.join(PKG, LIB_NAME)
 EXAMPLES_PATH = os.path.join(PKG, "libmallocmc_examples.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["heap_capi.cu", "workloads.cu", "batch.cu"]
+SOURCES = ["heap_capi.cu", "workloads.cu", "batch.cu", "serve.cu"]
 EXAMPLE_SOURCES = ["cxx_examples.cu"]  # user-side code on the C++ API, linked against the library
+TOOLS = ["verify_heap"]  # executables on the C++ API (csrc/<name>.cu -> mallocmc_gb300/<name>)
 
 
 def nvcc() -> str:
@@ -64,6 +65,13 @@ def build(verbose: bool = False, ptxas_verbose: bool = False) -> str:
         ex_objs.append(o)
         if _stale(o, [s] + hdrs):
             jobs.append([nvcc()] + _flags() + ["-c", s, "-o", o])
+    tool_objs = []
+    for name in TOOLS:
+        s = os.path.join(CSRC, name + ".cu")
+        o = os.path.join(BUILD_DIR, name + ".o")
+        tool_objs.append((name, o))
+        if _stale(o, [s] + hdrs):
+            jobs.append([nvcc()] + _flags() + ["-c", s, "-o", o])
     for src in SOURCES:
         s = os.path.join(CSRC, src)
         o = os.path.join(BUILD_DIR, src.replace(".cu", ".o"))
@@ -93,6 +101,14 @@ def build(verbose: bool = False, ptxas_verbose: bool = False) -> str:
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    for name, o in tool_objs:
+        exe = os.path.join(PKG, name)
+        if _stale(exe, [o, LIB_PATH]):
+            cmd = [nvcc()] + ARCH + ["-cudart", "static", "-o", exe, o, "-L" + PKG, "-lmallocmc_gb300",
+                                     "-Xlinker", "-rpath,$ORIGIN"]
+            r = subprocess.run(cmd, capture_output=True, text=True)
+            if r.returncode != 0:
+                raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
     return LIB_PATH
 
 

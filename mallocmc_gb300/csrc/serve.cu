@@ -1,0 +1,356 @@
+/* serve.cu — a continuous-batching request server on a device-resident heap.
+ *
+ * A request is a sequence of 2-byte elements that grows to a final length; it
+ * holds one 16 KiB chunk (malloc'd from the heap) per 256 elements, writes its
+ * elements (a seeded function of request and index) into them, and when it
+ * reaches its final length reads them all back into a checksum and frees its
+ * chunks. All request state lives on the device in a slot table.
+ *
+ * One tick = one launch (replayed from a captured CUDA graph in the batched
+ * form): it applies the host's admissions and slot releases for this tick,
+ * grows every live request by `step` elements (one warp per slot), completes
+ * the requests that reach their length, and refreshes the free-slot count of
+ * 16 KiB chunks that the host admits against. The per-request form launches
+ * one grow kernel per live request instead.
+ */
+#include "mmc_internal.h"
+
+#include <cstring>
+#include <new>
+#include <vector>
+
+using namespace mmc::host;
+namespace dv = mmc::dev;
+
+namespace
+{
+    constexpr uint32_t kChunkBytes = 16384;
+    constexpr uint32_t kElemsPerChunk = 256;
+
+    __host__ __device__ __forceinline__ uint64_t mix64(uint64_t seed, uint64_t a, uint64_t b)
+    {
+        uint64_t z = seed + a * 0x9E3779B97F4A7C15ull + b * 0xD1B54A32D192ED03ull;
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        return z ^ (z >> 31);
+    }
+} // namespace
+
+struct mmc_server
+{
+    mmc_heap* heap;
+    mmc_device_handle handle;
+    int device;
+    uint32_t slots;
+    uint32_t max_chunks;
+    uint32_t step;
+    uint32_t queue_cap;
+    mmc_serve_slot* d_slots;   /* slot table */
+    void** d_chunks;           /* slots x max_chunks chunk pointers */
+    mmc_serve_cmd* d_queue;    /* this tick's admissions / releases */
+    uint32_t* d_queue_len;
+    mmc_serve_cmd* h_queue;    /* pinned staging of the queue */
+    uint32_t* h_queue_len;     /* pinned */
+    mmc_serve_slot* h_slots;   /* pinned copy of the slot table after each tick */
+    unsigned* d_free;          /* free 16 KiB slots after the tick */
+    unsigned* h_free;          /* pinned */
+    cudaStream_t stream;
+    cudaGraphExec_t exec;
+    cudaGraph_t graph;
+};
+
+/* Apply admissions (cmd.kind 1) and releases (cmd.kind 2). */
+__global__ void mmc_serve_apply(mmc_serve_slot* slots, const mmc_serve_cmd* q, const uint32_t* qlen)
+{
+    const uint32_t n = *qlen;
+    for(uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    {
+        const mmc_serve_cmd c = q[i];
+        mmc_serve_slot& s = slots[c.slot];
+        if(c.kind == 1u)
+        {
+            s.id = c.id;
+            s.final_len = c.final_len;
+            s.len = 0u;
+            s.nchunks = 0u;
+            s.seed = c.seed;
+            s.failed = 0u;
+            s.checksum = 0ull;
+            s.state = MMC_SERVE_LIVE;
+        }
+        else if(c.kind == 2u)
+            s.state = MMC_SERVE_FREE;
+    }
+}
+
+/* Grow one live request by `step` elements (one warp), completing it at its length. */
+__device__ __forceinline__ void grow_request(const mmc_device_handle& h, mmc_serve_slot& s, void** chunks,
+                                             uint32_t max_chunks, uint32_t step)
+{
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t len = s.len;
+    const uint32_t end = min(len + step, s.final_len);
+    uint32_t failed = 0u;
+    /* chunks this step needs: one per 256-element boundary crossed */
+    const uint32_t first_chunk = (len + kElemsPerChunk - 1u) / kElemsPerChunk;
+    const uint32_t last_chunk = (end + kElemsPerChunk - 1u) / kElemsPerChunk; /* exclusive */
+    for(uint32_t c = first_chunk + lane; c < last_chunk && c < max_chunks; c += 32u)
+    {
+        void* p = dv::malloc<dv::GpuIds>(h, kChunkBytes);
+        chunks[c] = p;
+        failed += p == nullptr;
+    }
+    failed = __reduce_add_sync(0xFFFFFFFFu, failed);
+    __syncwarp();
+    if(failed == 0u)
+    {
+        for(uint32_t e = len + lane; e < end; e += 32u)
+        {
+            uint16_t* chunk = static_cast<uint16_t*>(chunks[e / kElemsPerChunk]);
+            chunk[e % kElemsPerChunk] = static_cast<uint16_t>(mix64(s.seed, e, 0x5E7ull));
+        }
+    }
+    else
+    {
+        /* give back what this step took; the request retries next tick */
+        for(uint32_t c = first_chunk + lane; c < last_chunk && c < max_chunks; c += 32u)
+            if(chunks[c])
+                dv::free<dv::GpuIds>(h, chunks[c]);
+    }
+    __syncwarp();
+    if(lane == 0u)
+    {
+        if(failed)
+            s.failed += 1u;
+        else
+        {
+            s.len = end;
+            s.nchunks = last_chunk;
+        }
+    }
+    __syncwarp();
+    if(failed == 0u && end == s.final_len)
+    {
+        /* complete: read every element back, checksum, free the chunks */
+        unsigned long long sum = 0ull;
+        for(uint32_t e = lane; e < end; e += 32u)
+        {
+            const uint16_t v = static_cast<const uint16_t*>(chunks[e / kElemsPerChunk])[e % kElemsPerChunk];
+            sum += static_cast<unsigned long long>(v) * (e + 1ull);
+        }
+        for(int off = 16; off > 0; off >>= 1)
+            sum += __shfl_down_sync(0xFFFFFFFFu, sum, off);
+        __syncwarp();
+        for(uint32_t c = lane; c < last_chunk; c += 32u)
+            dv::free<dv::GpuIds>(h, chunks[c]);
+        if(lane == 0u)
+        {
+            s.checksum = sum;
+            s.state = MMC_SERVE_DONE;
+        }
+    }
+}
+
+/* Batched tick: one warp per slot. */
+__global__ void __launch_bounds__(256) mmc_serve_tick_kernel(mmc_device_handle h, mmc_serve_slot* slots,
+                                                             void** chunks, uint32_t nslots, uint32_t max_chunks,
+                                                             uint32_t step)
+{
+    const uint32_t warps = gridDim.x * (blockDim.x / 32u);
+    for(uint32_t w = blockIdx.x * (blockDim.x / 32u) + threadIdx.x / 32u; w < nslots; w += warps)
+    {
+        if(slots[w].state != MMC_SERVE_LIVE)
+            continue;
+        grow_request(h, slots[w], chunks + static_cast<uint64_t>(w) * max_chunks, max_chunks, step);
+    }
+}
+
+/* Per-request form: one warp, one slot. */
+__global__ void mmc_serve_one_kernel(mmc_device_handle h, mmc_serve_slot* slots, void** chunks, uint32_t slot,
+                                     uint32_t max_chunks, uint32_t step)
+{
+    if(slots[slot].state != MMC_SERVE_LIVE)
+        return;
+    grow_request(h, slots[slot], chunks + static_cast<uint64_t>(slot) * max_chunks, max_chunks, step);
+}
+
+namespace
+{
+    void release(mmc_server* s)
+    {
+        if(s == nullptr)
+            return;
+        if(s->exec)
+            cudaGraphExecDestroy(s->exec);
+        if(s->graph)
+            cudaGraphDestroy(s->graph);
+        if(s->stream)
+            cudaStreamDestroy(s->stream);
+        cudaFree(s->d_slots);
+        cudaFree(s->d_chunks);
+        cudaFree(s->d_queue);
+        cudaFree(s->d_queue_len);
+        cudaFree(s->d_free);
+        cudaFreeHost(s->h_queue);
+        cudaFreeHost(s->h_queue_len);
+        cudaFreeHost(s->h_slots);
+        cudaFreeHost(s->h_free);
+        delete s;
+    }
+
+    /* The tick's stream work: queue upload, apply, grow (batched) or not,
+     * free-slot count, slot table and count download. */
+    mmc_status enqueue_tick(mmc_server* s, bool batched)
+    {
+        cudaStream_t st = s->stream;
+        cudaMemcpyAsync(s->d_queue_len, s->h_queue_len, sizeof(uint32_t), cudaMemcpyHostToDevice, st);
+        cudaMemcpyAsync(s->d_queue, s->h_queue, sizeof(mmc_serve_cmd) * s->queue_cap, cudaMemcpyHostToDevice, st);
+        mmc_serve_apply<<<8, 128, 0, st>>>(s->d_slots, s->d_queue, s->d_queue_len);
+        if(batched)
+        {
+            const uint32_t blocks = (s->slots + 7u) / 8u;
+            mmc_serve_tick_kernel<<<blocks, 256, 0, st>>>(s->handle, s->d_slots, s->d_chunks, s->slots, s->max_chunks,
+                                                         s->step);
+        }
+        mmc_status r = mmc_available_slots_async(s->heap, kChunkBytes, st, s->d_free);
+        if(r != MMC_OK)
+            return r;
+        cudaMemcpyAsync(s->h_slots, s->d_slots, sizeof(mmc_serve_slot) * s->slots, cudaMemcpyDeviceToHost, st);
+        cudaMemcpyAsync(s->h_free, s->d_free, sizeof(unsigned), cudaMemcpyDeviceToHost, st);
+        return cuda_check(cudaGetLastError(), "serve tick");
+    }
+} // namespace
+
+extern "C" {
+
+mmc_status mmc_serve_create(mmc_heap* heap, uint32_t slots, uint32_t max_chunks, uint32_t step, uint32_t queue_cap,
+                            mmc_server** out)
+{
+    if(heap == nullptr || out == nullptr || slots == 0u || max_chunks == 0u || step == 0u || queue_cap == 0u)
+        return fail(MMC_ERR_ARG, "bad server parameters");
+    *out = nullptr;
+    mmc_server* s = new(std::nothrow) mmc_server();
+    if(s == nullptr)
+        return fail(MMC_ERR_OOM, "host allocation failed");
+    s->heap = heap;
+    mmc_heap_device_handle(heap, &s->handle);
+    cudaGetDevice(&s->device);
+    s->slots = slots;
+    s->max_chunks = max_chunks;
+    s->step = step;
+    s->queue_cap = queue_cap;
+    mmc_status st = cuda_check(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking), "server stream");
+    if(st == MMC_OK)
+        st = cuda_check(cudaMalloc(&s->d_slots, sizeof(mmc_serve_slot) * slots), "slots");
+    if(st == MMC_OK)
+        st = cuda_check(cudaMalloc(&s->d_chunks, sizeof(void*) * static_cast<size_t>(slots) * max_chunks), "chunks");
+    if(st == MMC_OK)
+        st = cuda_check(cudaMalloc(&s->d_queue, sizeof(mmc_serve_cmd) * queue_cap), "queue");
+    if(st == MMC_OK)
+        st = cuda_check(cudaMalloc(&s->d_queue_len, sizeof(uint32_t)), "queue length");
+    if(st == MMC_OK)
+        st = cuda_check(cudaMalloc(&s->d_free, sizeof(unsigned)), "free count");
+    if(st == MMC_OK)
+        st = cuda_check(cudaMallocHost(&s->h_queue, sizeof(mmc_serve_cmd) * queue_cap), "pinned queue");
+    if(st == MMC_OK)
+        st = cuda_check(cudaMallocHost(&s->h_queue_len, sizeof(uint32_t)), "pinned queue length");
+    if(st == MMC_OK)
+        st = cuda_check(cudaMallocHost(&s->h_slots, sizeof(mmc_serve_slot) * slots), "pinned slots");
+    if(st == MMC_OK)
+        st = cuda_check(cudaMallocHost(&s->h_free, sizeof(unsigned)), "pinned free count");
+    if(st == MMC_OK)
+        st = cuda_check(cudaMemset(s->d_slots, 0, sizeof(mmc_serve_slot) * slots), "zero slots");
+    if(st == MMC_OK)
+        st = cuda_check(cudaMemset(s->d_chunks, 0, sizeof(void*) * static_cast<size_t>(slots) * max_chunks),
+                        "zero chunks");
+    if(st != MMC_OK)
+    {
+        release(s);
+        return st;
+    }
+    *s->h_queue_len = 0u;
+    *s->h_free = 0u;
+    std::memset(s->h_slots, 0, sizeof(mmc_serve_slot) * slots);
+    /* capture the batched tick once */
+    st = cuda_check(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
+    if(st == MMC_OK)
+    {
+        mmc_status e = enqueue_tick(s, true);
+        st = cuda_check(cudaStreamEndCapture(s->stream, &s->graph), "end capture");
+        if(st == MMC_OK)
+            st = e;
+    }
+    if(st == MMC_OK)
+        st = cuda_check(cudaGraphInstantiate(&s->exec, s->graph, 0), "instantiate tick graph");
+    if(st != MMC_OK)
+    {
+        release(s);
+        return st;
+    }
+    *out = s;
+    return MMC_OK;
+}
+
+mmc_status mmc_serve_queue(mmc_server* s, mmc_serve_cmd** queue, uint32_t** queue_len, mmc_serve_slot** slots,
+                           unsigned** free_chunks)
+{
+    if(s == nullptr)
+        return fail(MMC_ERR_ARG, "server is null");
+    if(queue)
+        *queue = s->h_queue;
+    if(queue_len)
+        *queue_len = s->h_queue_len;
+    if(slots)
+        *slots = s->h_slots;
+    if(free_chunks)
+        *free_chunks = s->h_free;
+    return MMC_OK;
+}
+
+mmc_status mmc_serve_tick(mmc_server* s, int batched)
+{
+    if(s == nullptr)
+        return fail(MMC_ERR_ARG, "server is null");
+    mmc_status st = MMC_OK;
+    if(batched)
+        st = cuda_check(cudaGraphLaunch(s->exec, s->stream), "tick graph launch");
+    else
+    {
+        /* one grow launch per live request (from the host copy of the table),
+         * around the same apply / count / download steps */
+        cudaStream_t stream = s->stream;
+        cudaMemcpyAsync(s->d_queue_len, s->h_queue_len, sizeof(uint32_t), cudaMemcpyHostToDevice, stream);
+        cudaMemcpyAsync(s->d_queue, s->h_queue, sizeof(mmc_serve_cmd) * s->queue_cap, cudaMemcpyHostToDevice, stream);
+        mmc_serve_apply<<<8, 128, 0, stream>>>(s->d_slots, s->d_queue, s->d_queue_len);
+        for(uint32_t i = 0; i < *s->h_queue_len; ++i)
+            if(s->h_queue[i].kind == 1u)
+                s->h_slots[s->h_queue[i].slot].state = MMC_SERVE_LIVE;
+        for(uint32_t w = 0; w < s->slots; ++w)
+            if(s->h_slots[w].state == MMC_SERVE_LIVE)
+                mmc_serve_one_kernel<<<1, 32, 0, stream>>>(s->handle, s->d_slots, s->d_chunks, w, s->max_chunks,
+                                                           s->step);
+        st = mmc_available_slots_async(s->heap, kChunkBytes, stream, s->d_free);
+        if(st == MMC_OK)
+        {
+            cudaMemcpyAsync(s->h_slots, s->d_slots, sizeof(mmc_serve_slot) * s->slots, cudaMemcpyDeviceToHost,
+                            stream);
+            cudaMemcpyAsync(s->h_free, s->d_free, sizeof(unsigned), cudaMemcpyDeviceToHost, stream);
+            st = cuda_check(cudaGetLastError(), "per-request tick");
+        }
+    }
+    if(st == MMC_OK)
+        st = cuda_check(cudaStreamSynchronize(s->stream), "tick");
+    return st;
+}
+
+mmc_status mmc_serve_destroy(mmc_server* s)
+{
+    if(s == nullptr)
+        return MMC_OK;
+    cudaSetDevice(s->device);
+    cudaStreamSynchronize(s->stream);
+    release(s);
+    return MMC_OK;
+}
+
+} /* extern "C" */

@@ -10,6 +10,8 @@
  */
 #include "mmc_internal.h"
 
+#include <algorithm>
+
 using namespace mmc::host;
 namespace dv = mmc::dev;
 
@@ -227,6 +229,113 @@ __global__ void __launch_bounds__(256) mmc_stress_oldmalloc_kernel(mmc_stress_pa
     }
 }
 
+/* ---------------------------------------------------------- fragmentation */
+
+/* oc_frag_size of the oracle, on the device. */
+__device__ __forceinline__ uint32_t frag_size(const mmc_frag_params& p, uint64_t i)
+{
+    const uint64_t m = mix64(p.seed, i, 0xF4A6ull);
+    if(static_cast<uint32_t>(m % 1000u) < p.large_permille)
+    {
+        const double u = static_cast<double>((m >> 20) & 0xFFFFFFull) / 16777216.0;
+        const double lo = static_cast<double>(p.large_lo), hi = static_cast<double>(p.large_hi);
+        const uint32_t s = static_cast<uint32_t>(lo * exp(u * log(hi / lo)));
+        return s < p.large_lo ? p.large_lo : (s > p.large_hi ? p.large_hi : s);
+    }
+    return p.small_lo + static_cast<uint32_t>((m >> 32) % static_cast<uint64_t>(p.small_hi - p.small_lo + 1u));
+}
+
+__device__ __forceinline__ uint64_t frag_tag(uint64_t slot, uint64_t off) { return (slot << 24) ^ off ^ 0xA5A5F00Dull; }
+
+/* tags every 4 KiB and at the last aligned u64 of the block */
+__device__ __forceinline__ void frag_write_tags(char* p, uint32_t size, uint64_t slot)
+{
+    for(uint32_t off = 0; off + 8u <= size; off += 4096u)
+        *reinterpret_cast<uint64_t*>(p + off) = frag_tag(slot, off);
+    const uint32_t last = (size & ~7u) - 8u;
+    *reinterpret_cast<uint64_t*>(p + last) = frag_tag(slot, last);
+}
+
+__device__ __forceinline__ unsigned long long frag_check_tags(const char* p, uint32_t size, uint64_t slot)
+{
+    unsigned long long bad = 0;
+    for(uint32_t off = 0; off + 8u <= size; off += 4096u)
+        bad += *reinterpret_cast<const uint64_t*>(p + off) != frag_tag(slot, off);
+    const uint32_t last = (size & ~7u) - 8u;
+    bad += *reinterpret_cast<const uint64_t*>(p + last) != frag_tag(slot, last);
+    return bad;
+}
+
+__global__ void __launch_bounds__(256) mmc_fill_kernel(mmc_device_handle h, mmc_frag_params p, void** ptrs,
+                                                       uint32_t* sizes, uint64_t capacity,
+                                                       unsigned long long* counters)
+{
+    const uint64_t T = static_cast<uint64_t>(gridDim.x) * blockDim.x;
+    const uint64_t t = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    unsigned long long made = 0, bytes = 0;
+    for(uint32_t k = 0; k < p.max_per_thread; ++k)
+    {
+        if(dv::ld_rlx(reinterpret_cast<const uint32_t*>(&counters[4])) != 0u)
+            break;
+        const uint32_t size = frag_size(p, p.first_request + t + k * T);
+        ++made;
+        char* ptr = static_cast<char*>(dv::malloc<dv::GpuIds>(h, size));
+        if(ptr == nullptr)
+        {
+            atomicExch(reinterpret_cast<unsigned*>(&counters[4]), 1u);
+            break;
+        }
+        const unsigned long long slot = atomicAdd(&counters[0], 1ull);
+        if(slot >= capacity)
+        {
+            dv::free<dv::GpuIds>(h, ptr);
+            atomicExch(reinterpret_cast<unsigned*>(&counters[4]), 1u);
+            break;
+        }
+        frag_write_tags(ptr, size, slot);
+        ptrs[slot] = ptr;
+        sizes[slot] = size;
+        bytes += size;
+    }
+    atomicAdd(&counters[1], bytes);
+    atomicAdd(&counters[2], made);
+}
+
+__global__ void mmc_free_list_kernel(mmc_device_handle h, void** ptrs, uint32_t* sizes, const uint32_t* idx,
+                                     uint64_t n, unsigned long long* counters)
+{
+    unsigned long long bytes = 0, bad = 0;
+    for(uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; i < n;
+        i += static_cast<uint64_t>(gridDim.x) * blockDim.x)
+    {
+        const uint32_t s = idx[i];
+        char* ptr = static_cast<char*>(ptrs[s]);
+        if(ptr == nullptr)
+            continue;
+        bad += frag_check_tags(ptr, sizes[s], s);
+        bytes += sizes[s];
+        dv::free<dv::GpuIds>(h, ptr);
+        ptrs[s] = nullptr;
+        sizes[s] = 0u;
+    }
+    if(bytes)
+        atomicAdd(&counters[1], 0ull - bytes);
+    if(bad)
+        atomicAdd(&counters[3], bad);
+}
+
+__global__ void mmc_verify_list_kernel(void* const* ptrs, const uint32_t* sizes, uint64_t n,
+                                       unsigned long long* counters)
+{
+    unsigned long long bad = 0;
+    for(uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; i < n;
+        i += static_cast<uint64_t>(gridDim.x) * blockDim.x)
+        if(ptrs[i] != nullptr)
+            bad += frag_check_tags(static_cast<const char*>(ptrs[i]), sizes[i], i);
+    if(bad)
+        atomicAdd(&counters[3], bad);
+}
+
 /* Verify workload: malloc(sizes[t]); write u32 (t ^ seed); optionally verify and free. */
 template<bool ALLOC, bool FREE>
 __global__ void mmc_verify_kernel(mmc_device_handle h, uint32_t nthreads, const uint32_t* sizes, uint32_t seed,
@@ -413,6 +522,47 @@ mmc_status mmc_run_free_offsets(mmc_heap* heap, uint32_t blocks, uint32_t tpb, c
     mmc_verify_kernel<false, true><<<blocks, tpb, 0, as_stream(stream)>>>(h, blocks * tpb, sizes, seed,
                                                                         const_cast<int64_t*>(offsets), errors);
     return cuda_check(cudaGetLastError(), "free kernel");
+}
+
+mmc_status mmc_run_fill(mmc_heap* heap, const mmc_frag_params* p, void** ptrs, uint32_t* sizes, uint64_t capacity,
+                        unsigned long long* counters, void* stream)
+{
+    if(heap == nullptr || p == nullptr || ptrs == nullptr || sizes == nullptr || counters == nullptr)
+        return fail(MMC_ERR_ARG, "null argument");
+    if(p->blocks == 0u || p->threads_per_block == 0u || p->threads_per_block > 256u || p->small_lo < 8u
+       || p->small_hi < p->small_lo || p->large_lo < 8u || p->large_hi < p->large_lo || p->large_permille > 1000u)
+        return fail(MMC_ERR_ARG, "bad fragmentation parameters");
+    mmc_device_handle h;
+    mmc_heap_device_handle(heap, &h);
+    mmc_fill_kernel<<<p->blocks, p->threads_per_block, 0, as_stream(stream)>>>(h, *p, ptrs, sizes, capacity,
+                                                                               counters);
+    return cuda_check(cudaGetLastError(), "fill kernel");
+}
+
+mmc_status mmc_run_free_list(mmc_heap* heap, void** ptrs, uint32_t* sizes, const uint32_t* idx, uint64_t n,
+                             unsigned long long* counters, void* stream)
+{
+    if(heap == nullptr || ptrs == nullptr || sizes == nullptr || idx == nullptr || counters == nullptr)
+        return fail(MMC_ERR_ARG, "null argument");
+    if(n == 0u)
+        return MMC_OK;
+    mmc_device_handle h;
+    mmc_heap_device_handle(heap, &h);
+    const unsigned grid = static_cast<unsigned>(std::min<uint64_t>((n + 255u) / 256u, scan_grid(0) * 4u));
+    mmc_free_list_kernel<<<grid, 256, 0, as_stream(stream)>>>(h, ptrs, sizes, idx, n, counters);
+    return cuda_check(cudaGetLastError(), "free-list kernel");
+}
+
+mmc_status mmc_run_verify_list(mmc_heap* heap, void* const* ptrs, const uint32_t* sizes, uint64_t n,
+                               unsigned long long* counters, void* stream)
+{
+    if(heap == nullptr || ptrs == nullptr || sizes == nullptr || counters == nullptr)
+        return fail(MMC_ERR_ARG, "null argument");
+    if(n == 0u)
+        return MMC_OK;
+    const unsigned grid = static_cast<unsigned>(std::min<uint64_t>((n + 255u) / 256u, scan_grid(0) * 4u));
+    mmc_verify_list_kernel<<<grid, 256, 0, as_stream(stream)>>>(ptrs, sizes, n, counters);
+    return cuda_check(cudaGetLastError(), "verify-list kernel");
 }
 
 mmc_status mmc_atomic_peak(uint32_t* buf, uint64_t words, uint32_t blocks, uint32_t tpb, uint32_t iters,

@@ -1,0 +1,73 @@
+"""Fragmentation and large-allocation mix: fill until the first NULL, free a
+seeded half of the live blocks, refill until the next NULL; report the fill
+fraction (live requested bytes / heap bytes) and the throughput."""
+from __future__ import annotations
+
+import ctypes
+import time
+
+import numpy as np
+
+from . import _lib as L
+from .allocator import Allocator, _stream_ptr
+
+
+def frag_params(blocks, threads_per_block, seed, first_request=0, small=(16, 2048), large=(8192, 1 << 20),
+                large_permille=100, max_per_thread=1 << 16):
+    p = L.MmcFragParams()
+    p.blocks, p.threads_per_block, p.seed, p.first_request = blocks, threads_per_block, seed, first_request
+    p.small_lo, p.small_hi = small
+    p.large_lo, p.large_hi = large
+    p.large_permille, p.max_per_thread = large_permille, max_per_thread
+    return p
+
+
+def run_fragmentation(alloc: Allocator, seed: int, blocks: int, threads_per_block: int = 256,
+                      capacity: int = 1 << 22, small=(16, 2048), large=(8192, 1 << 20), large_permille=100,
+                      stream=None) -> dict:
+    import torch
+
+    lib = L.lib()
+    dev = torch.device("cuda", alloc.device)
+    s = _stream_ptr(stream)
+    ptrs = torch.zeros(capacity, dtype=torch.int64, device=dev)
+    sizes = torch.zeros(capacity, dtype=torch.int32, device=dev)
+    ctr = torch.zeros(8, dtype=torch.int64, device=dev)
+    heap_bytes = alloc.getHeapLocations()[0].size
+    out = {"heap_bytes": heap_bytes}
+
+    def fill(first):
+        p = frag_params(blocks, threads_per_block, seed, first, small, large, large_permille)
+        ctr[4] = 0
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        L.check(lib.mmc_run_fill(alloc.handle_ptr, ctypes.byref(p), ptrs.data_ptr(), sizes.data_ptr(), capacity,
+                                 ctr.data_ptr(), s), "fill")
+        torch.cuda.synchronize(dev)
+        return time.perf_counter() - t0
+
+    t1 = fill(0)
+    c = ctr.cpu().numpy().view(np.uint64)
+    n1, live1, req1 = int(c[0]), int(c[1]), int(c[2])
+    out.update(phase1_allocs=n1, phase1_requests=req1, phase1_live_bytes=live1, phase1_fill=live1 / heap_bytes,
+               phase1_seconds=t1)
+    half = np.random.default_rng(seed).permutation(min(n1, capacity))[: n1 // 2].astype(np.uint32)
+    idx = torch.from_numpy(half.view(np.int32)).to(dev)
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    L.check(lib.mmc_run_free_list(alloc.handle_ptr, ptrs.data_ptr(), sizes.data_ptr(), idx.data_ptr(), len(half),
+                                  ctr.data_ptr(), s), "free_list")
+    torch.cuda.synchronize(dev)
+    tf = time.perf_counter() - t0
+    t2 = fill(1 << 40)
+    c = ctr.cpu().numpy().view(np.uint64)
+    n_total, live2, req_total = int(c[0]), int(c[1]), int(c[2])
+    L.check(lib.mmc_run_verify_list(alloc.handle_ptr, ptrs.data_ptr(), sizes.data_ptr(), min(n_total, capacity),
+                                    ctr.data_ptr(), s), "verify_list")
+    torch.cuda.synchronize(dev)
+    c = ctr.cpu().numpy().view(np.uint64)
+    ops = req_total + len(half)
+    out.update(freed=len(half), phase2_allocs=n_total - n1, final_live_bytes=live2, final_fill=live2 / heap_bytes,
+               tag_errors=int(c[3]), free_seconds=tf, phase2_seconds=t2,
+               ops_per_second=ops / (t1 + tf + t2), list_overflow=n_total > capacity)
+    return out

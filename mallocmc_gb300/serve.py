@@ -1,0 +1,144 @@
+"""Serving-style request loop on the device-resident heap (continuous batching).
+
+Requests arrive (Poisson), wait until the heap has enough free 16 KiB slots for
+their expected chunks (the device's getAvailableSlots count, refreshed every
+tick, minus the chunks already promised to live requests) and a server slot is
+free, then grow on the device tick by tick; completed requests hand back their
+checksum and their slot. Latency is admit-to-completion, measured on the host
+clock at the ticks that admit and complete a request.
+"""
+from __future__ import annotations
+
+import ctypes
+import time
+from collections import deque
+
+import numpy as np
+
+from . import _lib as L
+from .allocator import Allocator
+
+ELEMS_PER_CHUNK = 256
+SLOT_DTYPE = np.dtype([("id", "<u4"), ("final_len", "<u4"), ("len", "<u4"), ("nchunks", "<u4"), ("seed", "<u8"),
+                       ("state", "<u4"), ("failed", "<u4"), ("checksum", "<u8")])
+CMD_DTYPE = np.dtype([("kind", "<u4"), ("slot", "<u4"), ("id", "<u4"), ("final_len", "<u4"), ("seed", "<u8")])
+
+
+def make_requests(n: int, rate: float, seed: int = 5, median: int = 1024, sigma: float = 1.0, cap: int = 32768):
+    """n requests: Poisson arrivals at `rate`/s (exponential gaps), final lengths
+    lognormal (median, sigma) capped, per-request content seeds."""
+    rng = np.random.default_rng(seed)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, size=n))
+    lengths = np.minimum(np.maximum(1, np.round(np.exp(rng.normal(np.log(median), sigma, size=n)))), cap)
+    seeds = rng.integers(1, 2**62, size=n, dtype=np.int64)
+    return arrivals, lengths.astype(np.int64), seeds
+
+
+def expected_checksum(seed: int, length: int) -> int:
+    """The checksum a request of `length` elements computes: sum of value x (index + 1)."""
+    from oracle.oracle import mix64
+
+    e = np.arange(length, dtype=np.uint64)
+    v = (mix64(seed, e, 0x5E7) & np.uint64(0xFFFF)).astype(np.uint64)
+    return int((v * (e + np.uint64(1))).sum(dtype=np.uint64))
+
+
+class Server:
+    def __init__(self, alloc: Allocator, slots: int = 4096, max_chunks: int = 128, step: int = 64,
+                 queue_cap: int = 8192):
+        self.alloc = alloc
+        self.nslots = slots
+        self.max_chunks = max_chunks
+        self.step = step
+        self.queue_cap = queue_cap
+        self._s = ctypes.c_void_p()
+        L.check(L.lib().mmc_serve_create(alloc.handle_ptr, slots, max_chunks, step, queue_cap, ctypes.byref(self._s)),
+                "serve_create")
+        q, ql, sl, fr = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_void_p()
+        L.check(L.lib().mmc_serve_queue(self._s, ctypes.byref(q), ctypes.byref(ql), ctypes.byref(sl),
+                                        ctypes.byref(fr)), "serve_queue")
+        self.queue = np.ctypeslib.as_array(ctypes.cast(q, ctypes.POINTER(ctypes.c_uint8)),
+                                           shape=(queue_cap * CMD_DTYPE.itemsize,)).view(CMD_DTYPE)
+        self.queue_len = np.ctypeslib.as_array(ctypes.cast(ql, ctypes.POINTER(ctypes.c_uint32)), shape=(1,))
+        self.slots = np.ctypeslib.as_array(ctypes.cast(sl, ctypes.POINTER(ctypes.c_uint8)),
+                                           shape=(slots * SLOT_DTYPE.itemsize,)).view(SLOT_DTYPE)
+        self.free_chunks = np.ctypeslib.as_array(ctypes.cast(fr, ctypes.POINTER(ctypes.c_uint32)), shape=(1,))
+
+    def tick(self, batched: bool = True):
+        L.check(L.lib().mmc_serve_tick(self._s, int(batched)), "serve_tick")
+
+    def close(self):
+        if getattr(self, "_s", None):
+            L.lib().mmc_serve_destroy(self._s)
+            self._s = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def run(self, arrivals, lengths, seeds, batched: bool = True, realtime: bool = True, max_seconds: float = 60.0):
+        """Serve the requests; returns a dict of per-request admit / done times
+        (seconds from start), checksums, and loop counters. With realtime=False
+        every request is treated as arrived at the start (used by tests)."""
+        n = len(arrivals)
+        need = -(-lengths // ELEMS_PER_CHUNK)
+        admit_t = np.full(n, np.nan)
+        done_t = np.full(n, np.nan)
+        checksum = np.zeros(n, dtype=np.uint64)
+        waiting = deque()
+        nxt = 0
+        free_slots = list(range(self.nslots - 1, -1, -1))
+        released = []  # slots whose release is in this tick's queue: reusable from the next tick on
+        slot_req = np.full(self.nslots, -1, dtype=np.int64)
+        promised = 0  # chunks live requests will still take
+        ticks = 0
+        done = 0
+        # first tick: learn the free-slot count
+        self.queue_len[0] = 0
+        self.tick(batched)
+        t0 = time.perf_counter()
+        while done < n:
+            now = time.perf_counter() - t0
+            if now > max_seconds:
+                break
+            while nxt < n and (not realtime or arrivals[nxt] <= now):
+                waiting.append(nxt)
+                nxt += 1
+            cmds = 0
+            free_slots.extend(released)
+            released = []
+            # completions of the last tick
+            st = self.slots["state"]
+            for s in np.nonzero(st == L.MMC_SERVE_DONE)[0]:
+                r = slot_req[s]
+                if r >= 0:
+                    done_t[r] = now
+                    checksum[r] = self.slots["checksum"][s]
+                    done += 1
+                    slot_req[s] = -1
+                    released.append(int(s))
+                    self.queue[cmds] = (2, s, 0, 0, 0)
+                    cmds += 1
+            live = slot_req >= 0
+            promised = int((need[slot_req[live]] - self.slots["nchunks"][live]).sum()) if live.any() else 0
+            available = int(self.free_chunks[0]) - promised
+            while waiting and free_slots and cmds < self.queue_cap:
+                r = waiting[0]
+                if need[r] > available:
+                    break
+                waiting.popleft()
+                s = free_slots.pop()
+                slot_req[s] = r
+                self.queue[cmds] = (1, s, r, int(lengths[r]), int(seeds[r]))
+                cmds += 1
+                available -= int(need[r])
+                admit_t[r] = now
+            self.queue_len[0] = cmds
+            self.tick(batched)
+            ticks += 1
+            if not realtime and nxt >= n and not waiting and not (slot_req >= 0).any():
+                break
+        return {"admit": admit_t, "done": done_t, "checksum": checksum, "ticks": ticks,
+                "seconds": time.perf_counter() - t0, "completed": done}

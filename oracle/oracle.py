@@ -108,6 +108,9 @@ def lib():
         L.oc_run_stress.argtypes = [vp, u64, u32, u64, u32, u32, u32, ctypes.c_int,
                                     ctypes.POINTER(u64), ctypes.POINTER(u64), ctypes.POINTER(ctypes.c_double)]
         L.oc_run_stress.restype = u64
+        L.oc_frag_size.argtypes = [u64, u64, u32, u32, u32, u32, u32]
+        L.oc_frag_size.restype = u32
+        L.oc_run_fragmentation.argtypes = [vp, u64, u32, u32, u32, u32, u32, vp]
         _lib = L
     return _lib
 
@@ -203,6 +206,14 @@ class OracleHeap:
         m = None if masks is None else np.ascontiguousarray(masks, dtype=np.uint32)
         lib().oc_load_state(self._h, ptes.ctypes.data, None if r is None else r.ctypes.data,
                             None if m is None else m.ctypes.data)
+
+    def run_fragmentation(self, seed: int, small=(16, 2048), large=(8192, 1 << 20), large_permille: int = 100):
+        """The reference's fill / free-half / refill on this heap (see scatter_oracle.h)."""
+        out = np.zeros(6, dtype=np.uint64)
+        lib().oc_run_fragmentation(self._h, seed, small[0], small[1], large[0], large[1], large_permille,
+                                   out.ctypes.data)
+        keys = ("phase1_allocs", "phase1_live_bytes", "freed", "phase2_allocs", "final_live_bytes", "micros")
+        return {k: int(v) for k, v in zip(keys, out)}
 
     def run_stress(self, vthreads: int, rounds: int, seed: int, lo: int, hi: int, step: int, workers: int):
         nulls, bad, secs = ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_double()

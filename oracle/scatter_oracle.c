@@ -732,6 +732,86 @@ uint64_t oc_mix64(uint64_t seed, uint64_t a, uint64_t b)
     return z ^ (z >> 31);
 }
 
+uint32_t oc_frag_size(uint64_t seed, uint64_t i, uint32_t small_lo, uint32_t small_hi, uint32_t large_lo,
+                      uint32_t large_hi, uint32_t large_permille)
+{
+    const uint64_t m = oc_mix64(seed, i, 0xF4A6ull);
+    if((uint32_t) (m % 1000u) < large_permille)
+    {
+        /* log-uniform: exp2 of a uniform exponent, from 24 bits of the draw */
+        const double u = (double) ((m >> 20) & 0xFFFFFFull) / 16777216.0;
+        const double lo = (double) large_lo, hi = (double) large_hi;
+        double v = lo * __builtin_exp(u * __builtin_log(hi / lo));
+        uint32_t s = (uint32_t) v;
+        return s < large_lo ? large_lo : (s > large_hi ? large_hi : s);
+    }
+    return small_lo + (uint32_t) ((m >> 32) % (uint64_t) (small_hi - small_lo + 1u));
+}
+
+void oc_run_fragmentation(oc_heap* h, uint64_t seed, uint32_t small_lo, uint32_t small_hi, uint32_t large_lo,
+                          uint32_t large_hi, uint32_t large_permille, uint64_t* out)
+{
+    struct timespec t0, t1;
+    clock_gettime(CLOCK_MONOTONIC, &t0);
+    size_t cap = 1u << 20, n = 0;
+    void** ptr = (void**) malloc(cap * sizeof(void*));
+    uint32_t* sz = (uint32_t*) malloc(cap * sizeof(uint32_t));
+    uint64_t i = 0, live = 0;
+    for(;; ++i)
+    {
+        const uint32_t s = oc_frag_size(seed, i, small_lo, small_hi, large_lo, large_hi, large_permille);
+        void* p = oc_malloc(h, s);
+        if(!p)
+            break;
+        if(n == cap)
+        {
+            cap *= 2;
+            ptr = (void**) realloc(ptr, cap * sizeof(void*));
+            sz = (uint32_t*) realloc(sz, cap * sizeof(uint32_t));
+        }
+        ptr[n] = p;
+        sz[n] = s;
+        ++n;
+        live += s;
+    }
+    out[0] = n;
+    out[1] = live;
+    /* seeded Fisher-Yates over the live list; free the first half */
+    for(size_t k = n; k > 1; --k)
+    {
+        const size_t j = (size_t) (oc_mix64(seed, k, 0x5A11ull) % k);
+        void* tp = ptr[k - 1];
+        ptr[k - 1] = ptr[j];
+        ptr[j] = tp;
+        uint32_t ts = sz[k - 1];
+        sz[k - 1] = sz[j];
+        sz[j] = ts;
+    }
+    const size_t half = n / 2;
+    for(size_t k = 0; k < half; ++k)
+    {
+        oc_free(h, ptr[k]);
+        live -= sz[k];
+    }
+    out[2] = half;
+    uint64_t n2 = 0;
+    for(++i;; ++i)
+    {
+        const uint32_t s = oc_frag_size(seed, i, small_lo, small_hi, large_lo, large_hi, large_permille);
+        void* p = oc_malloc(h, s);
+        if(!p)
+            break;
+        ++n2;
+        live += s;
+    }
+    out[3] = n2;
+    out[4] = live;
+    clock_gettime(CLOCK_MONOTONIC, &t1);
+    out[5] = (uint64_t) (1e6 * ((double) (t1.tv_sec - t0.tv_sec) + 1e-9 * (double) (t1.tv_nsec - t0.tv_nsec)));
+    free(ptr);
+    free(sz);
+}
+
 /* ---- multi-threaded stress (the CPU baseline) ---- */
 typedef struct
 {

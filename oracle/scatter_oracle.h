@@ -103,6 +103,21 @@ uint64_t oc_mix64(uint64_t seed, uint64_t a, uint64_t b);
 uint64_t oc_run_stress(oc_heap* h, uint64_t vthreads, uint32_t rounds, uint64_t seed, uint32_t lo, uint32_t hi,
                        uint32_t step, int workers, uint64_t* nulls, uint64_t* bad, double* seconds);
 
+/* Size of request i of the fragmentation workload: with probability
+ * large_permille / 1000 log-uniform in [large_lo, large_hi], else uniform in
+ * [small_lo, small_hi] (identical draw in C, CUDA and numpy). */
+uint32_t oc_frag_size(uint64_t seed, uint64_t i, uint32_t small_lo, uint32_t small_hi, uint32_t large_lo,
+                      uint32_t large_hi, uint32_t large_permille);
+
+/* The fragmentation workload run serially: phase 1 allocates requests 0, 1, ...
+ * until the first NULL; then a seeded half of the live blocks (a Fisher-Yates
+ * permutation of the live list, first half) is freed; phase 2 allocates
+ * requests first_null+1, ... until the next NULL. out[0..5] = {phase-1
+ * allocations, phase-1 live bytes, freed blocks, phase-2 allocations, final
+ * live bytes, seconds x 1e6}. Live bytes count requested sizes. */
+void oc_run_fragmentation(oc_heap* h, uint64_t seed, uint32_t small_lo, uint32_t small_hi, uint32_t large_lo,
+                          uint32_t large_hi, uint32_t large_permille, uint64_t* out);
+
 #ifdef __cplusplus
 }
 #endif

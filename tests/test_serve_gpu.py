@@ -1,0 +1,56 @@
+"""The continuous-batching request loop on the device-resident heap.
+
+Every request's checksum (over all its elements, read back before its chunks
+are freed) must equal the host's formula, whether it ran alone or in a mix of
+requests admitted while others were on the GPU, in the batched (one graph
+launch per tick) and in the per-request form. Afterwards the heap is clean."""
+import numpy as np
+import pytest
+
+from oracle.oracle import HeapConfig
+from tests.test_parity_gpu import gpu_allocator
+from tests.test_verify_gpu import assert_all_free
+
+pytestmark = pytest.mark.gpu
+
+
+def _server_heap():
+    return gpu_allocator(HeapConfig(65536, 512 << 20, 16, 2, False), 2 << 30)
+
+
+def test_mix_and_alone_checksums_equal():
+    from mallocmc_gb300.serve import Server, expected_checksum, make_requests
+
+    arrivals, lengths, seeds = make_requests(96, rate=1e9, seed=7)
+    want = np.array([expected_checksum(int(s), int(n)) for s, n in zip(seeds, lengths)], dtype=np.uint64)
+    with _server_heap() as alloc:
+        srv = Server(alloc, slots=64, max_chunks=128, step=64, queue_cap=256)
+        mix = srv.run(arrivals, lengths, seeds, batched=True, realtime=False)
+        assert mix["completed"] == len(arrivals)
+        assert np.array_equal(mix["checksum"], want)
+        per = srv.run(arrivals, lengths, seeds, batched=False, realtime=False)
+        assert per["completed"] == len(arrivals)
+        assert np.array_equal(per["checksum"], want)
+        for i in (0, 5, 17):
+            alone = srv.run(arrivals[i:i + 1], lengths[i:i + 1], seeds[i:i + 1], batched=True, realtime=False)
+            assert alone["checksum"][0] == want[i]
+        srv.close()
+        assert_all_free(alloc.snapshot(), pagesize=65536)
+        assert alloc.error_flags() == 0
+
+
+def test_admission_waits_for_free_chunks():
+    """A heap too small for all requests at once: admission must hold requests
+    back until completions return chunks, and every request still completes."""
+    from mallocmc_gb300.serve import Server, expected_checksum, make_requests
+
+    arrivals, lengths, seeds = make_requests(40, rate=1e9, seed=8, median=8192, sigma=0.3)
+    want = np.array([expected_checksum(int(s), int(n)) for s, n in zip(seeds, lengths)], dtype=np.uint64)
+    with gpu_allocator(HeapConfig(65536, 8 << 20, 16, 2, False), 16 << 20) as alloc:
+        srv = Server(alloc, slots=64, max_chunks=128, step=256, queue_cap=128)
+        res = srv.run(arrivals, lengths, seeds, batched=True, realtime=False)
+        assert res["completed"] == len(arrivals)
+        assert np.array_equal(res["checksum"], want)
+        # never more chunks promised than the heap held: some requests had to wait
+        assert np.nanmax(res["admit"]) > 0.0
+        srv.close()
