@@ -62,6 +62,7 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target length of the CPU baseline sample")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--no-frag", action="store_true")
     ap.add_argument("--serve-seconds", type=float, default=1.0, help="arrival window per rate of the serving loop")
     ap.add_argument("--autotune", action="store_true", help="re-run the batched workload's autotuner first")
     return ap.parse_args()
@@ -351,6 +352,51 @@ def serving_column(torch, args):
             "latency": "admit to completion (host clock at the admitting and completing ticks)", "rows": rows}
 
 
+FRAG_GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tests", "golden", "frag_fill.json")
+
+
+def fragmentation_column(torch, args, sms):
+    """Fill until the first NULL, free a seeded half, refill until the next NULL
+    on a 32 GiB heap (pagesize 4096, 256 MiB access blocks): 90 % of requests
+    uniform in [16, 2048] B, 10 % log-uniform in [8 KiB, 1 MiB]. Requests go out
+    in waves of SMs x 2 x 256 (one per thread). The reference's fill is the
+    oracle's serial run on the same seed and geometry, recorded in
+    tests/golden/frag_fill.json (ten minutes of CPU at this size). Run with the
+    hash distances tuned for fill (hashingDistMP 1, WP 0, WPRel 0) and with the
+    reference's defaults."""
+    from mallocmc_gb300 import AlignmentPolicies, Allocator, CreationPolicies, DistributionPolicies
+    from mallocmc_gb300.fragmentation import run_fragmentation
+
+    heap_bytes, ab, seed = 32 << 30, 256 << 20, 42
+    ref = None
+    if os.path.exists(FRAG_GOLDEN):
+        with open(FRAG_GOLDEN) as f:
+            doc = json.load(f)
+        for g in doc["geometries"]:
+            if g["heap_bytes"] == heap_bytes and g["accessblocksize"] == ab and doc["seed"] == seed:
+                ref = {"phase1_fill": g["phase1_fill"], "final_fill": g["final_fill"],
+                       "phase1_allocs": g["phase1_allocs"], "phase2_allocs": g["phase2_allocs"],
+                       "source": "oracle (serial reference algorithm), tests/golden/frag_fill.json"}
+    runs = {}
+    for label, (mp, wp, wprel) in (("tuned_hash", (1, 0, 0)), ("reference_hash", (17497, 1, 1))):
+        creation = CreationPolicies.Scatter(pagesize=4096, accessblocksize=ab, regionsize=16, wastefactor=2,
+                                            hashingDistMP=mp, hashingDistWP=wp, hashingDistWPRel=wprel)
+        alloc = Allocator(creation, DistributionPolicies.XMallocSIMD(4096), None, None, AlignmentPolicies.Shrink(16),
+                          size=heap_bytes)
+        r = run_fragmentation(alloc, seed, sms * 2, 256, capacity=1 << 23)
+        r["error_flags"] = alloc.error_flags()
+        alloc.close()
+        r["hash"] = {"hashingDistMP": mp, "hashingDistWP": wp, "hashingDistWPRel": wprel}
+        if ref is not None:
+            r["fill_vs_reference"] = {"phase1": r["phase1_fill"] - ref["phase1_fill"],
+                                      "final": r["final_fill"] - ref["final_fill"]}
+        runs[label] = r
+    return {"workload": "32 GiB heap, pagesize 4096, access block 256 MiB; 90% uniform [16, 2048] B, 10% "
+                        "log-uniform [8 KiB, 1 MiB]; fill to first NULL, free seeded half, refill to next NULL",
+            "unit": "ops/s (mallocs incl. the failing ones + frees) and fill = live requested bytes / heap bytes",
+            "reference": ref, **runs}
+
+
 def cpu_port_run(heap_gib, threads_total, rounds, target_s, workers):
     """The oracle port of the reference's CPU backend on `workers` host threads,
     on a bounded sample (virtual threads x rounds) of the same workload."""
@@ -543,6 +589,9 @@ def main():
     serving = None
     if not args.no_serve:
         serving = serving_column(torch, args)
+    frag = None
+    if not args.no_frag:
+        frag = fragmentation_column(torch, args, sms)
     oldm = None
     if not args.no_oldmalloc:
         oldm = oldmalloc_column(torch, stream, heap_bytes, blocks, tpb, args.oldmalloc_rounds, d_sizes, flush, pattern)
@@ -569,7 +618,7 @@ def main():
                    "pairs_per_step": work["pairs"], "l2": "flushed between timed steps (512 MiB write)",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "roofline": roofline, "atomic_roofline": atomic, "cpu_baseline": cpu, "e2e": e2e,
-        "oldmalloc": oldm, "batched": batched, "serving": serving,
+        "oldmalloc": oldm, "batched": batched, "serving": serving, "fragmentation": frag,
         "gpu_launches": args.steps, "clocks": clk.summary(), "wall_s_timed": wall,
         "per_step_ms": ms,
     }

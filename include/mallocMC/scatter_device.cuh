@@ -110,6 +110,15 @@ namespace mmc
             asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
             return v;
         }
+        __device__ __forceinline__ uint4 ld_rlx_v4(const u32* p)
+        {
+            uint4 v;
+            asm volatile("ld.relaxed.gpu.global.v4.u32 {%0, %1, %2, %3}, [%4];"
+                         : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+                         : "l"(p)
+                         : "memory");
+            return v;
+        }
         __device__ __forceinline__ void st_rlx(u32* p, u32 v)
         {
             asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
@@ -363,9 +372,57 @@ namespace mmc
             return r;
         }
 
+        /* The pages of one region a request may use, as two masks in page order
+         * (bit i = page region_offset + i): unformatted pages (chunk size 0) and
+         * pages formatted with a chunk size in [bytes, maxchunksize]. Every other
+         * page is one the reference's walk visits only to find it formatted for
+         * another size or taken by a multi-page run (Scatter.hpp:584-591). The
+         * chunk-size words are read with 16-byte loads, 16 pages in flight at
+         * once. Needs regionsize % 4 == 0 and regionsize <= 32. */
+        __device__ __forceinline__ void region_candidates(const mmc_device_handle& h, u32 region_offset, u32 bytes,
+                                                          u32 maxchunksize, u32& zero, u32& fit)
+        {
+            const u32 R = h.regionsize;
+            zero = 0u;
+            fit = 0u;
+            for(u32 base = 0; base < R; base += 16u)
+            {
+                uint4 v[4];
+#pragma unroll
+                for(u32 k = 0; k < 4u; ++k)
+                    v[k] = (base + 4u * k < R) ? ld_rlx_v4(&h.chunksize[region_offset + base + 4u * k])
+                                               : make_uint4(~0u, ~0u, ~0u, ~0u);
+#pragma unroll
+                for(u32 k = 0; k < 4u; ++k)
+                {
+                    const u32 w[4] = {v[k].x, v[k].y, v[k].z, v[k].w};
+#pragma unroll
+                    for(u32 j = 0; j < 4u; ++j)
+                    {
+                        const u32 bit = base + 4u * k + j;
+                        if(bit < 32u)
+                        {
+                            zero |= (w[j] == 0u ? 1u : 0u) << bit;
+                            fit |= ((w[j] >= bytes && w[j] <= maxchunksize) ? 1u : 0u) << bit;
+                        }
+                    }
+                }
+            }
+        }
+
         /* allocChunked's two-pass region walk (Scatter.hpp:563-636), resumed after
          * the first page: in the first region of pass 0 the region counter is
-         * the one already read (fill0) and the start page was already tried. */
+         * the one already read (fill0) and the start page was already tried.
+         *
+         * That first region is walked page by page, as the reference walks it
+         * (most walks end there, after a page or two). Every further region is
+         * read whole first (region_candidates: one round trip for 16 pages) and
+         * only its usable pages are tried, in the reference's order from the
+         * entry page: a walk that crosses regions of full pages or of multi-page
+         * runs (the page-based area, where region counters stay low because
+         * only failed chunk walks raise them) then costs one round trip per
+         * region instead of one per page. Alone on the heap every page gets the
+         * reference's outcome, in the reference's order. */
         template<class Ids>
         __device__ void* alloc_chunked_walk(const mmc_device_handle& h, u32 bytes, u32 minAllocation,
                                             u32 maxchunksize, u32 global_start_page, u32 fill0)
@@ -373,6 +430,8 @@ namespace mmc
             const u32 R = h.regionsize;
             const u32 numpages = h.numpages;
             const u32 pagesperblock = h.pagesperblock;
+            const bool batched = (R % 4u) == 0u && R <= 32u;
+            const u32 rmask = R >= 32u ? 0xFFFFFFFFu : ((1u << R) - 1u);
             u32 checklevel = R * 3u / 4u;
             for(u32 finder = 0; finder < 2u; ++finder)
             {
@@ -385,21 +444,44 @@ namespace mmc
                     const u32 region_offset = region * R;
                     if(regionfilllevel < checklevel)
                     {
-                        u32 page_in_region = global_page;
-                        bool skip = resumed;
-                        do
+                        if(batched && !resumed)
                         {
-                            if(!skip)
+                            u32 zero, fit;
+                            region_candidates(h, region_offset, bytes, maxchunksize, zero, fit);
+                            /* rotate so that bit i is the i-th page visited from the entry page */
+                            const u32 s0 = global_page - region_offset;
+                            const u32 z = s0 == 0u ? zero : (((zero >> s0) | (zero << (R - s0))) & rmask);
+                            const u32 f = s0 == 0u ? fit : (((fit >> s0) | (fit << (R - s0))) & rmask);
+                            for(u32 todo = z | f; todo != 0u; todo &= todo - 1u)
                             {
+                                const u32 i = static_cast<u32>(__ffs(static_cast<int>(todo))) - 1u;
+                                const u32 page = region_offset + (s0 + i) % R;
                                 MMC_STAT(h, MMC_STAT_WALK_PAGES);
-                                void* res = attempt_page<Ids>(h, page_in_region, ld_rlx(&h.chunksize[page_in_region]),
-                                                              bytes, minAllocation, maxchunksize);
+                                const u32 before = ((z >> i) & 1u) ? 0u : ld_rlx(&h.chunksize[page]);
+                                void* res = attempt_page<Ids>(h, page, before, bytes, minAllocation, maxchunksize);
                                 if(res != nullptr)
                                     return res;
                             }
-                            skip = false;
-                            page_in_region = region_offset + ((page_in_region + 1u) % R);
-                        } while(page_in_region != global_page);
+                        }
+                        else
+                        {
+                            u32 page_in_region = global_page;
+                            bool skip = resumed;
+                            do
+                            {
+                                if(!skip)
+                                {
+                                    MMC_STAT(h, MMC_STAT_WALK_PAGES);
+                                    void* res = attempt_page<Ids>(h, page_in_region,
+                                                                  ld_rlx(&h.chunksize[page_in_region]), bytes,
+                                                                  minAllocation, maxchunksize);
+                                    if(res != nullptr)
+                                        return res;
+                                }
+                                skip = false;
+                                page_in_region = region_offset + ((page_in_region + 1u) % R);
+                            } while(page_in_region != global_page);
+                        }
 
                         if(regionfilllevel + 1u <= R)
                             atomicCAS(&h.regions[region], regionfilllevel, regionfilllevel + 1u);
@@ -527,7 +609,9 @@ namespace mmc
             return page < h.numpages ? ld_rlx(&h.chunksize[page]) : 1u;
         }
 
-        /* markpages, Scatter.hpp:745-764 */
+        /* markpages, Scatter.hpp:745-764 (the serial form): CAS(chunksize,
+         * 0 -> bytes) page by page; on a failure the pages already set are put
+         * back with CAS(bytes -> 0). */
         __device__ inline bool markpages(const mmc_device_handle& h, u32 startpage, u32 pages, u32 bytes)
         {
             u32 abord = 0xFFFFFFFFu;
@@ -611,18 +695,72 @@ namespace mmc
             return res;
         }
 
+        /* What the concurrent page-based search needs of the handle. */
+        struct PageScan
+        {
+            u32* chunksize;
+            mmc_heap_state* state;
+            char* pages;
+            u32 numpages;
+            u32 pagesize;
+        };
+
+        /* markpages (Scatter.hpp:745-764) for concurrent callers: the CASes go
+         * out 4 at a time (independent atomics in flight together, not one
+         * round trip per page); on a failure every page this call set is put
+         * back with CAS(bytes -> 0), as the reference's roll-back does. With no
+         * concurrent caller the outcome is the serial form's. */
+        __device__ __forceinline__ bool markpages_batched(const PageScan& c, u32 startpage, u32 pages, u32 bytes)
+        {
+            const u32 end = startpage + pages;
+            for(u32 base = startpage; base < end; base += 4u)
+            {
+                u32 old[4];
+#pragma unroll
+                for(u32 k = 0; k < 4u; ++k)
+                    old[k] = (base + k < end) ? atomicCAS(&c.chunksize[base + k], 0u, bytes) : 0u;
+                u32 lost = 0u;
+#pragma unroll
+                for(u32 k = 0; k < 4u; ++k)
+                    lost |= (old[k] != 0u ? 1u : 0u) << k;
+                if(lost != 0u)
+                {
+                    for(u32 trypage = startpage; trypage < base; ++trypage)
+                        atomicCAS(&c.chunksize[trypage], bytes, 0u);
+#pragma unroll
+                    for(u32 k = 0; k < 4u; ++k)
+                        if(base + k < end && ((lost >> k) & 1u) == 0u)
+                            atomicCAS(&c.chunksize[base + k], bytes, 0u);
+                    return false;
+                }
+            }
+            return true;
+        }
+
         /* allocPageBasedSingleRegion's search (Scatter.hpp:775-813) for concurrent
          * callers, without the global mutex. The chunk-size words are read 16 pages
          * at a time (independent loads issued together, not one round trip per
          * page), free runs are counted exactly as the reference counts them
          * (downward, reset at a used page), and markpages' CAS decides who owns a
          * run. A lane that loses a run to a concurrent claim starts counting again
-         * below it. With no concurrent caller this finds the reference's run and
-         * updates the hint as the reference does. */
-        __device__ inline void* alloc_page_based_scan(const mmc_device_handle& h, u32 startpage, u32 endpage,
-                                                      u32 bytes)
+         * below it.
+         *
+         * The hint: the reference lowers firstFreePageBased to just below the new
+         * run when the search passed no used page (left_free), with a CAS from the
+         * value it started at. Many lanes start from one hint at once, and all
+         * but one of them pass runs their neighbours just claimed, so with that
+         * rule the hint would stay put while the claimed area under it grows and
+         * every later search walks it again. Here a run lost to a concurrent
+         * claim does not count as passed free space: a lane lowers the hint
+         * (atomicMin) to just below its run unless it left a free page behind
+         * above it. Alone on the heap, a search that passed no used page
+         * lowers the hint as the reference does; one that passed used pages with
+         * no free page between them and its run lowers it too (the pages above
+         * are all in use), where the reference keeps it. */
+        __device__ __forceinline__ char* alloc_page_based_scan(const PageScan& c, u32 startpage, u32 endpage,
+                                                               u32 bytes)
         {
-            const u32 pagestoalloc = divup(bytes, h.pagesize);
+            const u32 pagestoalloc = divup(bytes, c.pagesize);
             u32 freecount = 0;
             bool left_free = false;
             /* the reference visits startpage down to endpage, both included
@@ -636,7 +774,7 @@ namespace mmc
                 for(u32 k = 0; k < 16u; ++k)
                 {
                     const u32 q = top - 1u - k;
-                    v[k] = (q >= lo && q < h.numpages) ? __ldcg(&h.chunksize[q]) : 1u;
+                    v[k] = (q >= lo && q < c.numpages) ? __ldcg(&c.chunksize[q]) : 1u;
                 }
 #pragma unroll
                 for(u32 k = 0; k < 16u; ++k)
@@ -648,24 +786,19 @@ namespace mmc
                     {
                         if(++freecount == pagestoalloc)
                         {
-                            if(q + pagestoalloc <= h.numpages && markpages(h, q, pagestoalloc, bytes))
+                            if(q + pagestoalloc <= c.numpages && markpages_batched(c, q, pagestoalloc, bytes))
                             {
-                                if(!left_free)
-                                {
-                                    u32 nf = q - 1u;
-                                    if(!h.reference_quirks && q == 0u)
-                                        nf = 0u;
-                                    atomicCAS(&h.state->firstFreePageBased, startpage, nf);
-                                }
-                                return page_data(h, q);
+                                if(!left_free && q != 0u)
+                                    atomicMin(&c.state->firstFreePageBased, q - 1u);
+                                return c.pages + static_cast<u64>(q) * c.pagesize;
                             }
-                            freecount = 0u;
-                            left_free = true;
+                            freecount = 0u; /* a concurrent claim took these pages */
                         }
                     }
                     else
                     {
-                        left_free = true;
+                        if(freecount != 0u)
+                            left_free = true; /* free pages left behind above */
                         freecount = 0u;
                     }
                 }
@@ -674,21 +807,28 @@ namespace mmc
             return nullptr;
         }
 
+        /* allocPageBased, Scatter.hpp:848-866, for concurrent callers: every
+         * lane searches at once, lock-free (alloc_page_based_scan), where the
+         * reference's mutex serialises every large request of the GPU and each
+         * search walks the page table one round trip per page. */
+        __device__ inline char* alloc_page_based_concurrent(const PageScan& c, u32 bytes)
+        {
+            const u32 spage = ld_rlx(&c.state->firstFreePageBased);
+            char* res = alloc_page_based_scan(c, spage, 0u, bytes);
+            if(res == nullptr)
+                res = alloc_page_based_scan(c, c.numpages, spage, bytes);
+            return res;
+        }
+
         /* allocPageBased, Scatter.hpp:848-866. Alone on the heap (SerialIds) this
-         * is the reference's mutex-serialised search. With real thread ids every
-         * lane searches at once, lock-free (alloc_page_based_scan): the mutex
-         * serialised every large request in the GPU, and each search walks the
-         * page table one round trip per page. */
+         * is the reference's mutex-serialised search. */
         template<class Ids>
         __device__ void* alloc_page_based(const mmc_device_handle& h, u32 bytes)
         {
             if(Ids::warpSize == 1u)
                 return alloc_page_based_single(h, bytes);
-            const u32 spage = ld_rlx(&h.state->firstFreePageBased);
-            void* res = alloc_page_based_scan(h, spage, 0u, bytes);
-            if(res == nullptr)
-                res = alloc_page_based_scan(h, h.numpages, spage, bytes);
-            return res;
+            return alloc_page_based_concurrent(
+                PageScan{h.chunksize, h.state, h.pages, h.numpages, h.pagesize}, bytes);
         }
 
         /* deallocPageBased, Scatter.hpp:874-886 */

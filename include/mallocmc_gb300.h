@@ -297,8 +297,10 @@ mmc_status mmc_run_stress_oldmalloc(const mmc_stress_params* p, const uint16_t* 
  * fraction at out-of-memory under a mix of small and multi-page requests.
  * Request i of a phase has the size oracle/scatter_oracle.h's oc_frag_size
  * describes (with probability large_permille/1000 log-uniform in
- * [large_lo, large_hi], else uniform in [small_lo, small_hi]); thread t takes
- * requests first_request + t, + T, + 2T, ... (T threads). */
+ * [large_lo, large_hi], else uniform in [small_lo, small_hi]). Requests are
+ * made in waves, one request per thread per wave: in wave w thread t makes
+ * request first_request + w*T + t (T threads), so the live mix follows the
+ * request order the way a serial run's does, one wave at a time. */
 typedef struct mmc_frag_params
 {
     uint32_t blocks;
@@ -308,11 +310,12 @@ typedef struct mmc_frag_params
     uint32_t small_lo, small_hi;
     uint32_t large_lo, large_hi;
     uint32_t large_permille;
-    uint32_t max_per_thread; /* bound on one thread's requests in a phase */
+    uint32_t waves; /* waves one mmc_run_fill call launches (one kernel each) */
 } mmc_frag_params;
 
-/* Allocate until the first NULL anywhere (a device flag stops every thread
- * before its next request). Each block gets a u64 tag every 4 KiB and at its
+/* Allocate until the first NULL anywhere: a NULL sets a device flag, and the
+ * threads of later waves find it set and make no request (the requests of the
+ * wave that met the NULL all complete). Each block gets a u64 tag every 4 KiB and at its
  * end, and is appended to the list ptrs/sizes (capacity entries; counters[0]
  * is the list length, counters[1] the live requested bytes, counters[2] the
  * requests made, counters[3] tag errors, counters[4] the stop flag, which the

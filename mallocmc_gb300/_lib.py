@@ -71,7 +71,7 @@ class MmcServeCmd(ctypes.Structure):
 class MmcFragParams(ctypes.Structure):
     _fields_ = [("blocks", u32), ("threads_per_block", u32), ("seed", u64), ("first_request", u64),
                 ("small_lo", u32), ("small_hi", u32), ("large_lo", u32), ("large_hi", u32),
-                ("large_permille", u32), ("max_per_thread", u32)]
+                ("large_permille", u32), ("waves", u32)]
 
 
 # name -> (restype, argtypes); every function declared in include/mallocmc_gb300.h

@@ -29,7 +29,7 @@ def make_jobs(njobs: int = 512, seed: int = 3, tmin: int = 32, tmax: int = 65536
 
 def expected_pairs(jobs) -> np.ndarray:
     """Pairs each job performs (the cycle draws of the kernels, on the host)."""
-    from oracle.oracle import mix64
+    from .seeds import mix64
 
     out = np.zeros(len(jobs), dtype=np.int64)
     for i, j in enumerate(jobs):

@@ -12,10 +12,10 @@
  *
  * The allocator is the reference's (Scatter 4096 / 2 GiB / 16 / 2 / no reset,
  * Noop distribution, ReturnNull, Shrink 16). A heap below 2 GiB holds no whole
- * access block of that size; the reference then divides by zero
- * (Scatter.hpp:991-993) and this library refuses the configuration, so such
- * heaps run the same allocator with a 256 MiB access block (8 MiB below
- * 256 MiB), which -v reports.
+ * access block of that size (the page area is about 0.3 % smaller than the
+ * heap); the reference then divides by zero (Scatter.hpp:991-993) and this
+ * library refuses the configuration, so such heaps run the same allocator with
+ * a 256 MiB access block (8 MiB when even that does not fit), which -v reports.
  *
  * Additions: the content sum is also checked against the Gaussian sum of
  * 0 .. usedSlots*750-1 (the check the reference's comments describe,
@@ -339,10 +339,14 @@ int main(int argc, char** argv)
     bool correct = false;
     try
     {
-        if(heapMB >= 2048)
+        /* the page area of a heap of B bytes: floor(B / (regionsize * (12 + pagesize) + 4)) regions of
+         * regionsize pages (Scatter.hpp:976-980) */
+        const size_t heapBytes = size_t(1024U * 1024U) * heapMB;
+        const size_t pageArea = heapBytes / (16u * (12u + 4096u) + 4u) * 16u * 4096u;
+        if(pageArea >= (size_t(2) << 30))
             correct = run_heap_verification<2u * 1024u * 1024u * 1024u>(device, heapMB, blocks, threads,
                                                                         machine_readable);
-        else if(heapMB >= 256)
+        else if(pageArea >= (size_t(256) << 20))
         {
             dout() << "heap below one 2 GiB access block: using 256 MiB access blocks\n";
             correct = run_heap_verification<256u * 1024u * 1024u>(device, heapMB, blocks, threads, machine_readable);

@@ -60,8 +60,11 @@ __global__ void mmc_store_result_kernel(const unsigned* src, int64_t* dst) { *ds
  * block, cooperatively: the warp walks the blocks of its lanes in turn and
  * moves 512 contiguous bytes per instruction (16 per lane), instead of each
  * lane streaming its own block 16 bytes at a time across 32 cache lines.
- * Every lane of the warp must call it (blocks of lanes whose ptr is null are
- * skipped). Returns the pattern mismatches found in this lane's share. */
+ * The read-back takes the blocks four at a time and issues the first 1 KiB of
+ * all four before comparing, so a warp waits for one round trip per four
+ * blocks, not one per block. Every lane of the warp must call it (blocks of
+ * lanes whose ptr is null are skipped). Returns the pattern mismatches found
+ * in this lane's share. */
 __device__ __forceinline__ unsigned long long warp_pattern(char* ptr, uint32_t bytes, uint64_t m,
                                                            unsigned long long& csum)
 {
@@ -78,18 +81,54 @@ __device__ __forceinline__ unsigned long long warp_pattern(char* ptr, uint32_t b
             q[i] = make_ulonglong2(mk + 2u * i, mk + 2u * i + 1u);
     }
     __syncwarp();
-    for(unsigned rest = have; rest != 0u; rest &= rest - 1u)
+    constexpr uint32_t G = 4u; /* blocks per group */
+    for(unsigned rest = have; rest != 0u;)
     {
-        const int k = __ffs(static_cast<int>(rest)) - 1;
-        const ulonglong2* q
-            = reinterpret_cast<const ulonglong2*>(__shfl_sync(0xFFFFFFFFu, reinterpret_cast<unsigned long long>(ptr), k));
-        const uint32_t n16 = __shfl_sync(0xFFFFFFFFu, bytes, k) / 16u;
-        const uint64_t mk = __shfl_sync(0xFFFFFFFFu, m, k);
-        for(uint32_t i = lane; i < n16; i += 32u)
+        const ulonglong2* q[G];
+        uint32_t n16[G];
+        uint64_t mk[G];
+#pragma unroll
+        for(uint32_t j = 0; j < G; ++j)
         {
-            const ulonglong2 v = q[i];
-            bad += (v.x != mk + 2u * i) + (v.y != mk + 2u * i + 1u);
-            csum += v.x ^ v.y;
+            const int k = rest != 0u ? __ffs(static_cast<int>(rest)) - 1 : 0;
+            const bool live = rest != 0u;
+            rest &= rest - 1u;
+            q[j] = reinterpret_cast<const ulonglong2*>(
+                __shfl_sync(0xFFFFFFFFu, reinterpret_cast<unsigned long long>(ptr), k));
+            const uint32_t nk = __shfl_sync(0xFFFFFFFFu, bytes, k) / 16u;
+            n16[j] = live ? nk : 0u;
+            mk[j] = __shfl_sync(0xFFFFFFFFu, m, k);
+        }
+        /* units lane and lane + 32 of every block in the group, all loads in flight together */
+        ulonglong2 v[G][2];
+#pragma unroll
+        for(uint32_t j = 0; j < G; ++j)
+        {
+#pragma unroll
+            for(uint32_t u = 0; u < 2u; ++u)
+            {
+                const uint32_t i = lane + 32u * u;
+                v[j][u] = i < n16[j] ? q[j][i] : make_ulonglong2(mk[j] + 2u * i, mk[j] + 2u * i + 1u);
+            }
+        }
+#pragma unroll
+        for(uint32_t j = 0; j < G; ++j)
+        {
+#pragma unroll
+            for(uint32_t u = 0; u < 2u; ++u)
+            {
+                const uint32_t i = lane + 32u * u;
+                bad += (v[j][u].x != mk[j] + 2u * i) + (v[j][u].y != mk[j] + 2u * i + 1u);
+                if(i < n16[j])
+                    csum += v[j][u].x ^ v[j][u].y;
+            }
+            /* blocks above 1 KiB: the rest one 512-byte row at a time */
+            for(uint32_t i = lane + 64u; i < n16[j]; i += 32u)
+            {
+                const ulonglong2 w = q[j][i];
+                bad += (w.x != mk[j] + 2u * i) + (w.y != mk[j] + 2u * i + 1u);
+                csum += w.x ^ w.y;
+            }
         }
     }
     __syncwarp();
@@ -266,39 +305,33 @@ __device__ __forceinline__ unsigned long long frag_check_tags(const char* p, uin
     return bad;
 }
 
-__global__ void __launch_bounds__(256) mmc_fill_kernel(mmc_device_handle h, mmc_frag_params p, void** ptrs,
-                                                       uint32_t* sizes, uint64_t capacity,
+__global__ void __launch_bounds__(256) mmc_fill_kernel(mmc_device_handle h, mmc_frag_params p, uint64_t wave,
+                                                       void** ptrs, uint32_t* sizes, uint64_t capacity,
                                                        unsigned long long* counters)
 {
+    if(dv::ld_rlx(reinterpret_cast<const uint32_t*>(&counters[4])) != 0u)
+        return;
     const uint64_t T = static_cast<uint64_t>(gridDim.x) * blockDim.x;
     const uint64_t t = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-    unsigned long long made = 0, bytes = 0;
-    for(uint32_t k = 0; k < p.max_per_thread; ++k)
+    const uint32_t size = frag_size(p, p.first_request + wave * T + t);
+    char* ptr = static_cast<char*>(dv::malloc<dv::GpuIds>(h, size));
+    atomicAdd(&counters[2], 1ull);
+    if(ptr == nullptr)
     {
-        if(dv::ld_rlx(reinterpret_cast<const uint32_t*>(&counters[4])) != 0u)
-            break;
-        const uint32_t size = frag_size(p, p.first_request + t + k * T);
-        ++made;
-        char* ptr = static_cast<char*>(dv::malloc<dv::GpuIds>(h, size));
-        if(ptr == nullptr)
-        {
-            atomicExch(reinterpret_cast<unsigned*>(&counters[4]), 1u);
-            break;
-        }
-        const unsigned long long slot = atomicAdd(&counters[0], 1ull);
-        if(slot >= capacity)
-        {
-            dv::free<dv::GpuIds>(h, ptr);
-            atomicExch(reinterpret_cast<unsigned*>(&counters[4]), 1u);
-            break;
-        }
-        frag_write_tags(ptr, size, slot);
-        ptrs[slot] = ptr;
-        sizes[slot] = size;
-        bytes += size;
+        atomicExch(reinterpret_cast<unsigned*>(&counters[4]), 1u);
+        return;
     }
-    atomicAdd(&counters[1], bytes);
-    atomicAdd(&counters[2], made);
+    const unsigned long long slot = atomicAdd(&counters[0], 1ull);
+    if(slot >= capacity)
+    {
+        dv::free<dv::GpuIds>(h, ptr);
+        atomicExch(reinterpret_cast<unsigned*>(&counters[4]), 1u);
+        return;
+    }
+    frag_write_tags(ptr, size, slot);
+    ptrs[slot] = ptr;
+    sizes[slot] = size;
+    atomicAdd(&counters[1], static_cast<unsigned long long>(size));
 }
 
 __global__ void mmc_free_list_kernel(mmc_device_handle h, void** ptrs, uint32_t* sizes, const uint32_t* idx,
@@ -534,9 +567,15 @@ mmc_status mmc_run_fill(mmc_heap* heap, const mmc_frag_params* p, void** ptrs, u
         return fail(MMC_ERR_ARG, "bad fragmentation parameters");
     mmc_device_handle h;
     mmc_heap_device_handle(heap, &h);
-    mmc_fill_kernel<<<p->blocks, p->threads_per_block, 0, as_stream(stream)>>>(h, *p, ptrs, sizes, capacity,
-                                                                               counters);
-    return cuda_check(cudaGetLastError(), "fill kernel");
+    for(uint32_t w = 0; w < p->waves; ++w)
+    {
+        mmc_fill_kernel<<<p->blocks, p->threads_per_block, 0, as_stream(stream)>>>(h, *p, w, ptrs, sizes, capacity,
+                                                                                   counters);
+        const cudaError_t e = cudaGetLastError();
+        if(e != cudaSuccess)
+            return cuda_check(e, "fill kernel");
+    }
+    return MMC_OK;
 }
 
 mmc_status mmc_run_free_list(mmc_heap* heap, void** ptrs, uint32_t* sizes, const uint32_t* idx, uint64_t n,

@@ -13,18 +13,23 @@ from .allocator import Allocator, _stream_ptr
 
 
 def frag_params(blocks, threads_per_block, seed, first_request=0, small=(16, 2048), large=(8192, 1 << 20),
-                large_permille=100, max_per_thread=1 << 16):
+                large_permille=100, waves=8):
     p = L.MmcFragParams()
     p.blocks, p.threads_per_block, p.seed, p.first_request = blocks, threads_per_block, seed, first_request
     p.small_lo, p.small_hi = small
     p.large_lo, p.large_hi = large
-    p.large_permille, p.max_per_thread = large_permille, max_per_thread
+    p.large_permille, p.waves = large_permille, waves
     return p
 
 
 def run_fragmentation(alloc: Allocator, seed: int, blocks: int, threads_per_block: int = 256,
                       capacity: int = 1 << 22, small=(16, 2048), large=(8192, 1 << 20), large_permille=100,
-                      stream=None) -> dict:
+                      stream=None, waves_per_call: int = 8, max_waves: int = 1 << 20, release: bool = False) -> dict:
+    """Phase 1 fills from request 0 in waves of blocks*threads_per_block
+    requests until a wave meets a NULL; a seeded half of the live blocks is
+    freed; phase 2 continues with the next unused request index until the next
+    NULL. Returns fill fractions, counts, timings and the tag-error count. With
+    release, every block still live is then freed (its tags checked first)."""
     import torch
 
     lib = L.lib()
@@ -36,17 +41,26 @@ def run_fragmentation(alloc: Allocator, seed: int, blocks: int, threads_per_bloc
     heap_bytes = alloc.getHeapLocations()[0].size
     out = {"heap_bytes": heap_bytes}
 
+    T = blocks * threads_per_block
+
     def fill(first):
-        p = frag_params(blocks, threads_per_block, seed, first, small, large, large_permille)
+        """Waves from request `first` until the stop flag; returns (seconds, waves)."""
         ctr[4] = 0
         torch.cuda.synchronize(dev)
         t0 = time.perf_counter()
-        L.check(lib.mmc_run_fill(alloc.handle_ptr, ctypes.byref(p), ptrs.data_ptr(), sizes.data_ptr(), capacity,
-                                 ctr.data_ptr(), s), "fill")
+        waves = 0
+        while waves < max_waves:
+            p = frag_params(blocks, threads_per_block, seed, first + waves * T, small, large, large_permille,
+                            waves_per_call)
+            L.check(lib.mmc_run_fill(alloc.handle_ptr, ctypes.byref(p), ptrs.data_ptr(), sizes.data_ptr(),
+                                     capacity, ctr.data_ptr(), s), "fill")
+            waves += waves_per_call
+            if int(ctr[4].item()) != 0:
+                break
         torch.cuda.synchronize(dev)
-        return time.perf_counter() - t0
+        return time.perf_counter() - t0, waves
 
-    t1 = fill(0)
+    t1, w1 = fill(0)
     c = ctr.cpu().numpy().view(np.uint64)
     n1, live1, req1 = int(c[0]), int(c[1]), int(c[2])
     out.update(phase1_allocs=n1, phase1_requests=req1, phase1_live_bytes=live1, phase1_fill=live1 / heap_bytes,
@@ -59,7 +73,7 @@ def run_fragmentation(alloc: Allocator, seed: int, blocks: int, threads_per_bloc
                                   ctr.data_ptr(), s), "free_list")
     torch.cuda.synchronize(dev)
     tf = time.perf_counter() - t0
-    t2 = fill(1 << 40)
+    t2, w2 = fill(w1 * T)
     c = ctr.cpu().numpy().view(np.uint64)
     n_total, live2, req_total = int(c[0]), int(c[1]), int(c[2])
     L.check(lib.mmc_run_verify_list(alloc.handle_ptr, ptrs.data_ptr(), sizes.data_ptr(), min(n_total, capacity),
@@ -69,5 +83,14 @@ def run_fragmentation(alloc: Allocator, seed: int, blocks: int, threads_per_bloc
     ops = req_total + len(half)
     out.update(freed=len(half), phase2_allocs=n_total - n1, final_live_bytes=live2, final_fill=live2 / heap_bytes,
                tag_errors=int(c[3]), free_seconds=tf, phase2_seconds=t2,
-               ops_per_second=ops / (t1 + tf + t2), list_overflow=n_total > capacity)
+               ops_per_second=ops / (t1 + tf + t2), list_overflow=n_total > capacity, wave_requests=T,
+               waves=(w1, w2))
+    if release:
+        n = min(n_total, capacity)
+        every = torch.arange(n, dtype=torch.int32, device=dev)
+        L.check(lib.mmc_run_free_list(alloc.handle_ptr, ptrs.data_ptr(), sizes.data_ptr(), every.data_ptr(), n,
+                                      ctr.data_ptr(), s), "free_list")
+        torch.cuda.synchronize(dev)
+        c = ctr.cpu().numpy().view(np.uint64)
+        out.update(released_live_bytes=int(c[1]), tag_errors=int(c[3]))
     return out

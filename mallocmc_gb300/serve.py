@@ -36,7 +36,7 @@ def make_requests(n: int, rate: float, seed: int = 5, median: int = 1024, sigma:
 
 def expected_checksum(seed: int, length: int) -> int:
     """The checksum a request of `length` elements computes: sum of value x (index + 1)."""
-    from oracle.oracle import mix64
+    from .seeds import mix64
 
     e = np.arange(length, dtype=np.uint64)
     v = (mix64(seed, e, 0x5E7) & np.uint64(0xFFFF)).astype(np.uint64)

@@ -10,7 +10,9 @@ GOLDEN_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 
 def fixture_paths():
-    return sorted(glob.glob(os.path.join(GOLDEN_DIR, "*.json")))
+    """The op-program fixtures (gen_golden.py); frag_fill.json holds fill
+    fractions (gen_frag_golden.py), not a program."""
+    return sorted(p for p in glob.glob(os.path.join(GOLDEN_DIR, "*.json")) if os.path.basename(p) != "frag_fill.json")
 
 
 def load(path):

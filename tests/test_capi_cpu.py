@@ -109,3 +109,26 @@ def test_policy_constraints():
     c = make_config(CreationPolicies.Scatter(pagesize=16384, regionsize=8), DistributionPolicies.Noop(),
                     OOMPolicies.BadAllocException(), AlignmentPolicies.Noop())
     assert (c.pagesize, c.regionsize, c.distribution, c.oom_policy, c.dataAlignment) == (16384, 8, 0, 1, 1)
+
+
+def test_package_never_imports_the_oracle():
+    """The oracle is test infrastructure: no module of the product package names it."""
+    import glob
+    import os
+
+    pkg = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "mallocmc_gb300")
+    for path in glob.glob(os.path.join(pkg, "*.py")):
+        src = open(path).read()
+        assert "import oracle" not in src and "from oracle" not in src, path
+
+
+def test_seed_twin_matches_the_oracle_draws():
+    import numpy as np
+
+    from mallocmc_gb300.seeds import mix64
+    from oracle.oracle import lib, mix64 as oracle_mix64
+
+    a = np.arange(1000, dtype=np.uint64)
+    for seed, b in ((0, 0), (42, 0x5E7), (2**63 + 5, 0xC1C1E)):
+        assert np.array_equal(mix64(seed, a, b), oracle_mix64(seed, a, b))
+        assert int(mix64(seed, 7, b)) == lib().oc_mix64(seed, 7, b)

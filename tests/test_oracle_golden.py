@@ -75,3 +75,21 @@ def test_heap_smaller_than_access_block_is_rejected():
     """The reference divides by zero here (Scatter.hpp:991-993); the oracle reports a config error."""
     with pytest.raises(ValueError):
         OracleHeap(REF_CONFIGS["p4k_ab8m_r16_w2"], 4 << 20)
+
+
+def test_fragmentation_fixture_reproduces():
+    """tests/golden/frag_fill.json (gen_frag_golden.py) holds the oracle's fill on
+    the bench's fragmentation workload; the small geometry is recomputed here."""
+    import json
+    import os
+
+    from oracle.oracle import HeapConfig, OracleHeap
+
+    doc = json.load(open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "frag_fill.json")))
+    g = next(x for x in doc["geometries"] if x["heap_bytes"] == 1 << 30)
+    h = OracleHeap(HeapConfig(g["pagesize"], g["accessblocksize"], g["regionsize"], g["wastefactor"], False),
+                   g["heap_bytes"])
+    r = h.run_fragmentation(doc["seed"], tuple(doc["small"]), tuple(doc["large"]), doc["large_permille"])
+    for k in ("phase1_allocs", "phase1_live_bytes", "freed", "phase2_allocs", "final_live_bytes"):
+        assert r[k] == g[k], k
+    assert {x["heap_bytes"] for x in doc["geometries"]} >= {1 << 30, 32 << 30}

@@ -42,12 +42,14 @@ def _run_csv(*args):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("heap_mb,blocks,threads", [(1024, 64, 128), (2048, 152, 256), (64, 8, 32)])
+@pytest.mark.parametrize("heap_mb,blocks,threads", [(1024, 64, 128), (2048, 152, 256), (4096, 304, 256),
+                                                    (64, 8, 32)])
 def test_fill_verify_damage_free(heap_mb, blocks, threads):
     rc, v = _run_csv(f"--heapsize={heap_mb}", f"--blocks={blocks}", f"--threads={threads}")
     assert rc == 0 and v["correct"] == "1", v
     heap = heap_mb << 20
-    ab = (2 << 30) if heap_mb >= 2048 else (256 << 20) if heap_mb >= 256 else (8 << 20)
+    area = heap // (16 * (12 + 4096) + 4) * 16 * 4096
+    ab = (2 << 30) if area >= (2 << 30) else (256 << 20) if area >= (256 << 20) else (8 << 20)
     assert int(v["Accessblocks"]) == ab and int(v["heapsizeByte"]) == heap
     slot = 750 * 8
     assert int(v["maxSlots"]) == heap // slot
