@@ -42,7 +42,7 @@ SEED = 20261203
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--heap-gib", type=float, default=8.0)
@@ -126,10 +126,15 @@ class ClockSampler:
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "50"],
+                                          "--format=csv,noheader,nounits", "-lms", "20"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            # the timed region starts once nvidia-smi is sampling (its first line is out)
+            t0 = time.time()
+            while not self.lines and time.time() - t0 < 5.0:
+                time.sleep(0.01)
+            self.lines.clear()
         except FileNotFoundError:
             self.proc = None
         return self
@@ -362,7 +367,7 @@ def fragmentation_column(torch, args, sms):
     in waves of SMs x 2 x 256 (one per thread). The reference's fill is the
     oracle's serial run on the same seed and geometry, recorded in
     tests/golden/frag_fill.json (ten minutes of CPU at this size). Run with the
-    hash distances tuned for fill (hashingDistMP 1, WP 0, WPRel 0) and with the
+    hash distances tuned for fill (hashingDistMP, WP and WPRel 0) and with the
     reference's defaults."""
     from mallocmc_gb300 import AlignmentPolicies, Allocator, CreationPolicies, DistributionPolicies
     from mallocmc_gb300.fragmentation import run_fragmentation
@@ -378,7 +383,7 @@ def fragmentation_column(torch, args, sms):
                        "phase1_allocs": g["phase1_allocs"], "phase2_allocs": g["phase2_allocs"],
                        "source": "oracle (serial reference algorithm), tests/golden/frag_fill.json"}
     runs = {}
-    for label, (mp, wp, wprel) in (("tuned_hash", (1, 0, 0)), ("reference_hash", (17497, 1, 1))):
+    for label, (mp, wp, wprel) in (("tuned_hash", (0, 0, 0)), ("reference_hash", (17497, 1, 1))):
         creation = CreationPolicies.Scatter(pagesize=4096, accessblocksize=ab, regionsize=16, wastefactor=2,
                                             hashingDistMP=mp, hashingDistWP=wp, hashingDistWPRel=wprel)
         alloc = Allocator(creation, DistributionPolicies.XMallocSIMD(4096), None, None, AlignmentPolicies.Shrink(16),
@@ -407,9 +412,29 @@ def cpu_port_run(heap_gib, threads_total, rounds, target_s, workers):
     cal = heap.run_stress(4096, 4, SEED, 16, 1024, 16, workers)
     rate = cal["pairs"] / max(cal["seconds"], 1e-6)
     vthreads = int(min(threads_total, max(1024, target_s * rate / rounds)))
-    r = heap.run_stress(vthreads, rounds, SEED + 1, 16, 1024, 16, workers)
+    # whole steps repeated (new seeds) until the sample reaches target_s, when one step is shorter
+    total = {"pairs": 0, "nulls": 0, "bad": 0, "seconds": 0.0, "steps": 0}
+    while total["steps"] == 0 or total["seconds"] < target_s:
+        r = heap.run_stress(vthreads, rounds, SEED + 1 + total["steps"], 16, 1024, 16, workers)
+        for k in ("pairs", "nulls", "bad", "seconds"):
+            total[k] += r[k]
+        total["steps"] += 1
     heap.close()
-    return r, vthreads
+    return total, vthreads
+
+
+def stress_config(args, sms, world):
+    """The headline workload's `config`, shared by both arms of the bench."""
+    tpb = args.threads
+    return {"workload": f"uniform_stress_{args.heap_gib:g}GiB", "heap_bytes": int(args.heap_gib * (1 << 30)),
+            "grid": f"{sms}x{args.blocks_per_sm} blocks x {tpb} threads", "rounds": args.rounds,
+            "sizes": "uniform {16,32,...,1024} (u16 table in HBM)",
+            "pattern": (f"u64 pattern written and verified per block by its {args.pattern}"
+                        + (" (512 B per instruction)" if args.pattern == "warp" else " (16 B per store)")),
+            "policies": f"Scatter<4096,{args.accessblock_mib}MiB,16,2,noreset>+XMallocSIMD+ReturnNull+Shrink<16>",
+            "pairs_per_step": sms * args.blocks_per_sm * tpb * args.rounds,
+            "l2": "flushed between timed steps (512 MiB write)",
+            "parallelism": "replicas" if world > 1 else "single GPU"}
 
 
 def reference_arm(args):
@@ -442,12 +467,11 @@ def reference_arm(args):
         "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * r["seconds"], "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u32", "data": "synthetic (seeded SplitMix64 size draws)",
-        "config": {"workload": "uniform_stress", "heap_bytes": int(heap_gib * (1 << 30)), "rounds": args.rounds,
-                   "sizes": "uniform {16,32,...,1024}",
-                   "policies": "Scatter<4096,2GiB,16,2,noreset>+XMallocSIMD+ReturnNull+Shrink<16>"},
+        "config": stress_config(args, 152, args.gpus),
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": workers, "kind": "port",
-                         "sample": f"{vt} virtual threads x {args.rounds} rounds per step (alpaka CPU-backend "
-                                   f"semantics: warp size 1, smid = warpid = 0) on {workers} host threads"},
+                         "sample": f"per step {r['steps']} x ({vt} virtual threads x {args.rounds} rounds) of the "
+                                   f"workload (alpaka CPU-backend semantics: warp size 1, smid = warpid = 0; the "
+                                   f"oracle's 2 GiB access blocks) on {workers} host threads, about {per_step_s:g} s"},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "errors": {"nulls": r["nulls"], "pattern": r["bad"]},
     }
@@ -603,20 +627,13 @@ def main():
         except ValueError:
             r, vt = cpu_port_run(1.0, nthreads, rounds, args.cpu_seconds, workers)
         cpu = {"value": r["pairs"] / r["seconds"], "unit": UNIT, "cores": workers, "kind": "port",
-               "sample": f"{vt} virtual threads x {rounds} rounds (alpaka CPU-backend semantics) on {workers} host "
-                         f"threads, {r['seconds']:.1f} s"}
+               "sample": f"{r['steps']} x ({vt} virtual threads x {rounds} rounds) (alpaka CPU-backend semantics) "
+                         f"on {workers} host threads, {r['seconds']:.1f} s"}
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": per_step_ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
         "data": "synthetic (seeded SplitMix64 size draws)",
-        "config": {"workload": f"uniform_stress_{args.heap_gib:g}GiB", "heap_bytes": heap_bytes,
-                   "grid": f"{sms}x{args.blocks_per_sm} blocks x {tpb} threads", "rounds": rounds,
-                   "sizes": "uniform {16,32,...,1024} (u16 table in HBM)",
-                   "pattern": (f"u64 pattern written and verified per block by its {args.pattern}"
-                               + (" (512 B per instruction)" if args.pattern == "warp" else " (16 B per store)")),
-                   "policies": f"Scatter<4096,{args.accessblock_mib}MiB,16,2,noreset>+XMallocSIMD+ReturnNull+Shrink<16>",
-                   "pairs_per_step": work["pairs"], "l2": "flushed between timed steps (512 MiB write)",
-                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "config": stress_config(args, sms, world),
         "roofline": roofline, "atomic_roofline": atomic, "cpu_baseline": cpu, "e2e": e2e,
         "oldmalloc": oldm, "batched": batched, "serving": serving, "fragmentation": frag,
         "gpu_launches": args.steps, "clocks": clk.summary(), "wall_s_timed": wall,

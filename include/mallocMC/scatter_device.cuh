@@ -53,8 +53,10 @@ struct mmc_heap_state
 
 #ifdef MMC_DEVICE_STATS
 #define MMC_STAT(h, i) atomicAdd(&(h).state->stats[(i)], 1ull)
+#define MMC_STAT_ADD(h, i, n) atomicAdd(&(h).state->stats[(i)], static_cast<unsigned long long>(n))
 #else
 #define MMC_STAT(h, i) ((void) 0)
+#define MMC_STAT_ADD(h, i, n) ((void) 0)
 #endif
 
 namespace mmc
@@ -421,26 +423,49 @@ namespace mmc
          * entry page: a walk that crosses regions of full pages or of multi-page
          * runs (the page-based area, where region counters stay low because
          * only failed chunk walks raise them) then costs one round trip per
-         * region instead of one per page. Alone on the heap every page gets the
-         * reference's outcome, in the reference's order. */
+         * region instead of one per page. The region counters themselves are
+         * read eight regions ahead, so a stretch of regions skipped as 3/4 full
+         * costs one round trip per eight (a walk only changes the counter of the
+         * region it is in). Alone on the heap every page gets the reference's
+         * outcome, in the reference's order. */
         template<class Ids>
         __device__ void* alloc_chunked_walk(const mmc_device_handle& h, u32 bytes, u32 minAllocation,
                                             u32 maxchunksize, u32 global_start_page, u32 fill0)
         {
             const u32 R = h.regionsize;
             const u32 numpages = h.numpages;
+            const u32 numregions = h.numregions;
             const u32 pagesperblock = h.pagesperblock;
             const bool batched = (R % 4u) == 0u && R <= 32u;
             const u32 rmask = R >= 32u ? 0xFFFFFFFFu : ((1u << R) - 1u);
+            constexpr u32 kAhead = 8u;
             u32 checklevel = R * 3u / 4u;
             for(u32 finder = 0; finder < 2u; ++finder)
             {
                 u32 global_page = global_start_page;
+                u32 ahead[kAhead];
+                u32 ahead_left = 0u; /* counters of the next regions already read */
                 do
                 {
                     const u32 region = global_page / R;
                     const bool resumed = finder == 0u && global_page == global_start_page;
-                    const u32 regionfilllevel = resumed ? fill0 : ld_rlx(&h.regions[region]);
+                    if(!resumed && ahead_left == 0u)
+                    {
+#pragma unroll
+                        for(u32 k = 0; k < kAhead; ++k)
+                        {
+                            u32 r = region + k;
+                            r = r >= numregions ? r - numregions : r;
+                            ahead[k] = ld_rlx(&h.regions[r]);
+                        }
+                        ahead_left = kAhead;
+                    }
+                    u32 regionfilllevel = fill0;
+                    if(!resumed)
+                    {
+                        regionfilllevel = ahead[kAhead - ahead_left];
+                        --ahead_left;
+                    }
                     const u32 region_offset = region * R;
                     if(regionfilllevel < checklevel)
                     {
@@ -743,20 +768,10 @@ namespace mmc
          * page), free runs are counted exactly as the reference counts them
          * (downward, reset at a used page), and markpages' CAS decides who owns a
          * run. A lane that loses a run to a concurrent claim starts counting again
-         * below it.
-         *
-         * The hint: the reference lowers firstFreePageBased to just below the new
-         * run when the search passed no used page (left_free), with a CAS from the
-         * value it started at. Many lanes start from one hint at once, and all
-         * but one of them pass runs their neighbours just claimed, so with that
-         * rule the hint would stay put while the claimed area under it grows and
-         * every later search walks it again. Here a run lost to a concurrent
-         * claim does not count as passed free space: a lane lowers the hint
-         * (atomicMin) to just below its run unless it left a free page behind
-         * above it. Alone on the heap, a search that passed no used page
-         * lowers the hint as the reference does; one that passed used pages with
-         * no free page between them and its run lowers it too (the pages above
-         * are all in use), where the reference keeps it. */
+         * below it. The hint is updated as the reference updates it: lowered to
+         * just below the run by a CAS from the value the search started at, when
+         * the search passed no used page. With no concurrent caller this finds
+         * the reference's run. */
         __device__ __forceinline__ char* alloc_page_based_scan(const PageScan& c, u32 startpage, u32 endpage,
                                                                u32 bytes)
         {
@@ -769,6 +784,7 @@ namespace mmc
             while(top > endpage)
             {
                 const u32 lo = (top - endpage > 16u) ? top - 16u : endpage;
+                MMC_STAT_ADD(c, MMC_STAT_PAGE_SCAN, top - lo);
                 u32 v[16];
 #pragma unroll
                 for(u32 k = 0; k < 16u; ++k)
@@ -788,17 +804,18 @@ namespace mmc
                         {
                             if(q + pagestoalloc <= c.numpages && markpages_batched(c, q, pagestoalloc, bytes))
                             {
-                                if(!left_free && q != 0u)
-                                    atomicMin(&c.state->firstFreePageBased, q - 1u);
+                                if(!left_free)
+                                    atomicCAS(&c.state->firstFreePageBased, startpage, q - 1u);
                                 return c.pages + static_cast<u64>(q) * c.pagesize;
                             }
-                            freecount = 0u; /* a concurrent claim took these pages */
+                            MMC_STAT(c, MMC_STAT_PAGE_LOST);
+                            freecount = 0u;
+                            left_free = true;
                         }
                     }
                     else
                     {
-                        if(freecount != 0u)
-                            left_free = true; /* free pages left behind above */
+                        left_free = true;
                         freecount = 0u;
                     }
                 }
@@ -817,6 +834,8 @@ namespace mmc
             char* res = alloc_page_based_scan(c, spage, 0u, bytes);
             if(res == nullptr)
                 res = alloc_page_based_scan(c, c.numpages, spage, bytes);
+            if(res == nullptr)
+                MMC_STAT(c, MMC_STAT_PAGE_BASED_FAIL);
             return res;
         }
 

@@ -61,6 +61,9 @@ typedef enum mmc_status
 #define MMC_STAT_PAGE_FULL 6     /* pages tried whose chunks were all taken */
 #define MMC_STAT_CHUNKED_FAIL 7  /* chunked allocations that returned NULL */
 #define MMC_STAT_PAGE_BASED 8    /* multi-page allocations started */
+#define MMC_STAT_PAGE_SCAN 9     /* page-table words read by concurrent multi-page searches */
+#define MMC_STAT_PAGE_LOST 10    /* runs a concurrent multi-page search lost to another claim */
+#define MMC_STAT_PAGE_BASED_FAIL 11 /* concurrent multi-page allocations that returned NULL */
 #define MMC_STAT_COUNT 16
 
 /* Heap configuration: the template parameters of Scatter<HeapConfig, HashConfig>

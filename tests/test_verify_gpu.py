@@ -205,6 +205,50 @@ def test_stress_warp_pattern_mode():
         assert alloc.error_flags() == 0
 
 
+def _warp_pattern_checksum(sizes, seed, nthreads):
+    """What the warp pattern's read-back adds up: lane l of a warp reads units
+    l, l + 32, ... of every lane's block, sums (v.x ^ v.y) over them (u64, with
+    wrap) across all rounds; the lanes' sums are XORed within the warp and the
+    warps' results XORed together."""
+    from mallocmc_gb300.seeds import mix64
+
+    rounds = sizes.shape[0]
+    total = np.uint64(0)
+    with np.errstate(over="ignore"):
+        for w in range(nthreads // 32):
+            lane_sums = np.zeros(32, dtype=np.uint64)
+            for r in range(rounds):
+                t = np.arange(w * 32, w * 32 + 32, dtype=np.uint64)
+                m = mix64(seed, t, r)
+                for k in range(32):
+                    i = np.arange(int(sizes[r, w * 32 + k]) // 16, dtype=np.uint64)
+                    vx = m[k] + np.uint64(2) * i
+                    np.add.at(lane_sums, (i % np.uint64(32)).astype(np.int64), vx ^ (vx + np.uint64(1)))
+            x = np.uint64(0)
+            for v in lane_sums:
+                x ^= v
+            total ^= x
+    return int(total)
+
+
+def test_stress_warp_pattern_reads_back_every_unit():
+    """The warp pattern's read-back (staged through shared memory) sees every
+    16-byte unit it wrote: the kernel's checksum of the values read equals the
+    one computed from the sizes and seeds on the host."""
+    from mallocmc_gb300.workloads import PATTERN_WARP, run_stress
+
+    blocks, tpb, rounds, seed = 8, 256, 5, 77
+    n = blocks * tpb
+    rng = np.random.default_rng(5)
+    sizes = (rng.integers(1, 65, size=(rounds, n)) * 16).astype(np.uint16)
+    cfg = HeapConfig(4096, 64 << 20, 16, 2, False)
+    with gpu_allocator(cfg, 256 << 20) as alloc:
+        st = run_stress(alloc, blocks, tpb, rounds, 16, 1024, 16, seed=seed, write_pattern=PATTERN_WARP,
+                        sizes=sizes.ravel())
+        assert st["pairs"] == n * rounds and st["nulls"] == 0 and st["bad"] == 0
+        assert st["checksum"] == _warp_pattern_checksum(sizes, seed, n)
+
+
 def test_stress_full_size_steps_no_corruption():
     """The benchmark workload (8 GiB heap, SMs x 8 x 256 threads, 100 rounds of
     malloc / u64 pattern / verify / free) three times back to back: no block may
