@@ -140,6 +140,7 @@ __device__ __forceinline__ unsigned long long warp_pattern(char* ptr, uint32_t b
 /* Uniform stress: sizes[r * nthreads + t] or drawn from the seed. Launch
  * bounds of four 256-thread CTAs per SM (64 registers): that build measured
  * about 6 % faster on GB300 than the one without the bound. */
+template<uint32_t PATTERN>
 __global__ void __launch_bounds__(256, 4) mmc_stress_kernel(mmc_device_handle h, mmc_stress_params p,
                                                          const uint16_t* sizes, unsigned long long* stats)
 {
@@ -153,7 +154,7 @@ __global__ void __launch_bounds__(256, 4) mmc_stress_kernel(mmc_device_handle h,
         const uint32_t bytes
             = sizes ? sizes[r * nthreads + t] : p.lo + (static_cast<uint32_t>(m >> 32) % nsizes) * p.step;
         char* ptr = static_cast<char*>(dv::malloc<dv::GpuIds>(h, bytes));
-        if(p.write_pattern == MMC_PATTERN_WARP)
+        if constexpr(PATTERN == MMC_PATTERN_WARP)
         {
             /* every lane takes part, with or without a block */
             bad += warp_pattern(ptr, bytes, m, csum);
@@ -171,7 +172,7 @@ __global__ void __launch_bounds__(256, 4) mmc_stress_kernel(mmc_device_handle h,
             ++nulls;
             continue;
         }
-        if(p.write_pattern == MMC_PATTERN_THREAD)
+        if constexpr(PATTERN == MMC_PATTERN_THREAD)
         {
             /* 16-byte stores: chunks are 16-byte aligned under Shrink<16> */
             ulonglong2* q = reinterpret_cast<ulonglong2*>(ptr);
@@ -497,7 +498,13 @@ mmc_status mmc_run_stress(mmc_heap* heap, const mmc_stress_params* p, const uint
         return fail(MMC_ERR_ARG, "bad stress parameters");
     mmc_device_handle h;
     mmc_heap_device_handle(heap, &h);
-    mmc_stress_kernel<<<p->blocks, p->threads_per_block, 0, as_stream(stream)>>>(h, *p, sizes, stats);
+    /* one instantiation per pattern mode: only the mode's code is in the kernel */
+    if(p->write_pattern == MMC_PATTERN_WARP)
+        mmc_stress_kernel<MMC_PATTERN_WARP><<<p->blocks, p->threads_per_block, 0, as_stream(stream)>>>(h, *p, sizes,
+                                                                                                       stats);
+    else
+        mmc_stress_kernel<MMC_PATTERN_THREAD><<<p->blocks, p->threads_per_block, 0, as_stream(stream)>>>(h, *p, sizes,
+                                                                                                         stats);
     return cuda_check(cudaGetLastError(), "stress kernel");
 }
 
