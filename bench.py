@@ -111,6 +111,15 @@ def algorithmic_work(sizes: np.ndarray, pagesize: int = 4096):
             "metadata_bytes": meta, "bytes": payload + meta}
 
 
+# DRAM bytes (read + written) per malloc+free pair of the stress kernel, from one
+# ncu capture (dram__bytes_read.sum + dram__bytes_write.sum) of the same kernel on
+# a 2 GiB heap with 20 rounds (profiles/mmc_stress_kernel_uniform_2GiB_20rounds.md);
+# almost all of it is the write-back of the written payload, so it scales with pairs.
+STRESS_DRAM_BYTES_PER_PAIR = 587.0
+STRESS_TRAFFIC_NOTE = ("dram__bytes_read.sum + dram__bytes_write.sum per pair from an ncu capture of the same "
+                       "kernel on a 2 GiB heap / 20 rounds, times the pairs of one launch")
+
+
 class ClockSampler:
     """nvidia-smi samples during the timed region (clocks and throttle reasons)."""
 
@@ -597,7 +606,9 @@ def main():
     kernel_s = per_step_ms * 1e-3
     achieved_gbs = work["bytes"] / kernel_s / 1e9
     roofline = {"bound": "hbm", "achieved": achieved_gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                "frac": achieved_gbs / peaks["hbm_gbs"], "traffic": None, "peak_kind": peak_kind,
+                "frac": achieved_gbs / peaks["hbm_gbs"],
+                "traffic": STRESS_DRAM_BYTES_PER_PAIR * work["pairs"], "traffic_note": STRESS_TRAFFIC_NOTE,
+                "peak_kind": peak_kind,
                 "algorithmic_bytes_per_launch": work["bytes"], "payload_bytes_per_launch": work["payload_bytes"],
                 "metadata_bytes_per_launch": work["metadata_bytes"], "kernel": "mmc_stress_kernel"}
     atomic = None

@@ -735,7 +735,8 @@ namespace mmc
          * round trip per page); on a failure every page this call set is put
          * back with CAS(bytes -> 0), as the reference's roll-back does. With no
          * concurrent caller the outcome is the serial form's. */
-        __device__ __forceinline__ bool markpages_batched(const PageScan& c, u32 startpage, u32 pages, u32 bytes)
+        __device__ __forceinline__ bool markpages_batched(const PageScan& c, u32 startpage, u32 pages, u32 bytes,
+                                                          u32& free_below)
         {
             const u32 end = startpage + pages;
             for(u32 base = startpage; base < end; base += 4u)
@@ -756,6 +757,8 @@ namespace mmc
                     for(u32 k = 0; k < 4u; ++k)
                         if(base + k < end && ((lost >> k) & 1u) == 0u)
                             atomicCAS(&c.chunksize[base + k], bytes, 0u);
+                    /* the pages from startpage up to the lowest lost one were free */
+                    free_below = base + static_cast<u32>(__ffs(static_cast<int>(lost))) - 1u - startpage;
                     return false;
                 }
             }
@@ -767,8 +770,10 @@ namespace mmc
          * at a time (independent loads issued together, not one round trip per
          * page), free runs are counted exactly as the reference counts them
          * (downward, reset at a used page), and markpages' CAS decides who owns a
-         * run. A lane that loses a run to a concurrent claim starts counting again
-         * below it. The hint is updated as the reference updates it: lowered to
+         * run. A lane that loses a run to a concurrent claim keeps counting the
+         * free pages its markpages had held below the lost page, so no hole is
+         * left between its next run and the winner's. The hint is updated as the
+         * reference updates it: lowered to
          * just below the run by a CAS from the value the search started at, when
          * the search passed no used page. With no concurrent caller this finds
          * the reference's run. */
@@ -802,14 +807,17 @@ namespace mmc
                     {
                         if(++freecount == pagestoalloc)
                         {
-                            if(q + pagestoalloc <= c.numpages && markpages_batched(c, q, pagestoalloc, bytes))
+                            u32 free_below = 0u;
+                            if(q + pagestoalloc <= c.numpages
+                               && markpages_batched(c, q, pagestoalloc, bytes, free_below))
                             {
                                 if(!left_free)
                                     atomicCAS(&c.state->firstFreePageBased, startpage, q - 1u);
                                 return c.pages + static_cast<u64>(q) * c.pagesize;
                             }
                             MMC_STAT(c, MMC_STAT_PAGE_LOST);
-                            freecount = 0u;
+                            /* the run below the lost page is still free: keep counting it */
+                            freecount = free_below;
                             left_free = true;
                         }
                     }
