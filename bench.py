@@ -116,6 +116,10 @@ def algorithmic_work(sizes: np.ndarray, pagesize: int = 4096):
 # a 2 GiB heap with 20 rounds (profiles/mmc_stress_kernel_uniform_2GiB_20rounds.md);
 # almost all of it is the write-back of the written payload, so it scales with pairs.
 STRESS_DRAM_BYTES_PER_PAIR = 587.0
+# L2 atomic requests per pair counted by ncu (lts__t_requests_srcunit_tex_op_atom*
+# + op_red) in the same capture: below the reference algorithm's 4.72 because a
+# formatted page's chunk size is loaded instead of CAS'd.
+STRESS_NCU_ATOMICS_PER_PAIR = 4.04
 STRESS_TRAFFIC_NOTE = ("dram__bytes_read.sum + dram__bytes_write.sum per pair from an ncu capture of the same "
                        "kernel on a 2 GiB heap / 20 rounds, times the pairs of one launch")
 
@@ -617,6 +621,8 @@ def main():
         ach = work["atomics"] / kernel_s
         atomic = {"bound": "l2_atomic", "achieved": ach / 1e9, "peak": pk["atom_l2_32MiB"] / 1e9, "unit": "Gatomic/s",
                   "frac": ach / pk["atom_l2_32MiB"], "atomics_per_pair": work["atomics_per_pair"],
+                  "ncu_atomics_per_pair": STRESS_NCU_ATOMICS_PER_PAIR,
+                  "ncu_frac": work["pairs"] / kernel_s * STRESS_NCU_ATOMICS_PER_PAIR / pk["atom_l2_32MiB"],
                   "peaks_measured_gops": {k: v / 1e9 for k, v in pk.items()}}
     batched = None
     if not args.no_batched:

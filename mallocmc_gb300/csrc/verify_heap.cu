@@ -17,6 +17,10 @@
  * library refuses the configuration, so such heaps run the same allocator with
  * a 256 MiB access block (8 MiB when even that does not fit), which -v reports.
  *
+ * --blocks and --threads mean what the reference's help text says; the
+ * reference's main() passes them to run_heap_verification in swapped order
+ * (verify_heap.cpp:95 against :619), so its CSV shows --threads as Gridsize.
+ *
  * Additions: the content sum is also checked against the Gaussian sum of
  * 0 .. usedSlots*750-1 (the check the reference's comments describe,
  * verify_heap.cpp:495-498), and the heap's device error flags must be clear.

@@ -58,3 +58,33 @@ def test_fill_verify_damage_free(heap_mb, blocks, threads):
     # 6000-byte slots take two 4 KiB pages each: the heap holds numpages // 2 of them
     pages = OracleHeap(HeapConfig(4096, ab, 16, 2, False), heap).numpages
     assert pages // 2 * 0.99 <= used <= pages // 2
+
+
+def _reference_runs():
+    import json
+
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "verify_heap_ref.json")
+    return json.load(open(path))["runs"]
+
+
+def test_reference_fixture_is_well_formed():
+    for run in _reference_runs():
+        assert run["csv_header"] == HEADER and run["exit_status"] == 0
+        assert run["csv_values"].endswith(",1")  # the reference tool verified its own run
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("heap_mb", [4096, 8192])
+def test_matches_the_reference_tool(heap_mb):
+    """The reference's tests/verify_heap.cpp (recorded by gen_verify_heap_golden.py
+    on alpaka's CPU-serial backend) and this tool, same heap: the configuration
+    columns are equal; the fill of 6000-byte slots is within 1 % of the
+    reference's (concurrent multi-page claims may leave a few pages unused)."""
+    ref = next(r for r in _reference_runs() if r["heapsize_mb"] == heap_mb)
+    want = dict(zip(HEADER.split(","), ref["csv_values"].split(",")))
+    rc, got = _run_csv(f"--heapsize={heap_mb}", "--blocks=304", "--threads=256")
+    assert rc == 0 and got["correct"] == "1"
+    for col in ("PagesizeByte", "Accessblocks", "Regionsize", "ResetFreedPage", "ELEMS_PER_SLOT", "allocElemByte",
+                "heapsizeByte", "maxSpaceByte", "maxSlots", "correct"):
+        assert got[col] == want[col], col
+    assert int(want["usedSlots"]) * 0.99 <= int(got["usedSlots"]) <= int(want["usedSlots"])
