@@ -9,10 +9,14 @@ import numpy as np
 GOLDEN_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 
+# fixtures that are not op programs: fill fractions (gen_frag_golden.py) and the
+# reference verify_heap tool's CSV lines (gen_verify_heap_golden.py)
+NOT_PROGRAMS = {"frag_fill.json", "verify_heap_ref.json"}
+
+
 def fixture_paths():
-    """The op-program fixtures (gen_golden.py); frag_fill.json holds fill
-    fractions (gen_frag_golden.py), not a program."""
-    return sorted(p for p in glob.glob(os.path.join(GOLDEN_DIR, "*.json")) if os.path.basename(p) != "frag_fill.json")
+    """The op-program fixtures (gen_golden.py)."""
+    return sorted(p for p in glob.glob(os.path.join(GOLDEN_DIR, "*.json")) if os.path.basename(p) not in NOT_PROGRAMS)
 
 
 def load(path):
