@@ -436,6 +436,23 @@ def cpu_port_run(heap_gib, threads_total, rounds, target_s, workers):
     return total, vthreads
 
 
+def max_over_ranks(x: float, dist, device) -> float:
+    """The largest of every rank's x (the slowest rank's time); x itself on one rank."""
+    if dist is None:
+        return x
+    import torch
+
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_throughput(pairs_per_rank_step: int, world: int, slowest_ms_per_step: float) -> float:
+    """Whole-job pairs/s: every rank runs the same workload on its own heap
+    (replicas), so the job does world x the pairs in the slowest rank's time."""
+    return pairs_per_rank_step * world / (slowest_ms_per_step * 1e-3)
+
+
 def stress_config(args, sms, world):
     """The headline workload's `config`, shared by both arms of the bench."""
     tpb = args.threads
@@ -570,13 +587,9 @@ def main():
     st = stats.cpu().numpy().view(np.uint64)
     if int(st[0]) != work["pairs"] * args.steps or int(st[1]) or int(st[2]):
         raise RuntimeError(f"timed steps failed verification: {st.tolist()}")
-    total_ms = float(sum(ms))
-    if dist:
-        t = torch.tensor([total_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = max_over_ranks(float(sum(ms)), dist, "cuda")
     per_step_ms = total_ms / args.steps
-    value = work["pairs"] * world / (per_step_ms * 1e-3)
+    value = job_throughput(work["pairs"], world, per_step_ms)
 
     # ---- e2e: through the C ABI with host buffers ----
     e2e = None
@@ -592,12 +605,8 @@ def main():
             h_stats.copy_(stats, non_blocking=True)
             e1.record(stream)
         torch.cuda.synchronize()
-        e2e_ms = sum(e0.elapsed_time(e1) for e0, e1 in evs2) / args.steps
-        if dist:
-            t = torch.tensor([e2e_ms], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            e2e_ms = float(t.item())
-        e2e = {"value": work["pairs"] * world / (e2e_ms * 1e-3), "unit": UNIT,
+        e2e_ms = max_over_ranks(sum(e0.elapsed_time(e1) for e0, e1 in evs2) / args.steps, dist, "cuda")
+        e2e = {"value": job_throughput(work["pairs"], world, e2e_ms), "unit": UNIT,
                "h2d_bytes_per_step": int(sizes_np.nbytes), "d2h_bytes_per_step": int(h_stats.numel() * 8),
                "ms_per_step": e2e_ms}
 
