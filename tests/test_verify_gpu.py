@@ -188,6 +188,30 @@ def test_page_based_allocations_concurrent():
         assert alloc.error_flags() == 0
 
 
+def test_page_based_runs_above_256_pages_mixed_with_chunks():
+    """Full warps whose lanes ask for 1-3 MiB runs (256-768 pages: the warp's
+    claim spans several 256-page groups) next to lanes asking for 64-byte
+    chunks: no overlap, patterns intact, everything released."""
+    from mallocmc_gb300.workloads import alloc_offsets, free_offsets
+
+    cfg = HeapConfig(4096, 256 << 20, 16, 2, False)
+    n = 4 * 64
+    rng = np.random.default_rng(11)
+    big = (16 * rng.integers((1 << 20) // 16, (3 << 20) // 16, size=n)).astype(np.uint32)
+    sizes = np.where(np.arange(n) % 2 == 0, big, 64).astype(np.uint32)
+    with gpu_allocator(cfg, 1 << 30) as alloc:
+        g = alloc.geometry()
+        ds, offs_t = alloc_offsets(alloc, 4, 64, sizes, 12)
+        offs = offs_t.cpu().numpy()
+        assert np.all(offs >= 0)
+        check_live_blocks(offs, sizes, g.numpages, 4096)
+        assert free_offsets(alloc, 4, 64, ds, offs_t, 12) == 0
+        ptes, regions, masks, hdr = alloc.snapshot()
+        assert int(ptes[:, 0].max()) <= 4096
+        assert_all_free((ptes, regions, masks, hdr))
+        assert alloc.error_flags() == 0
+
+
 def test_stress_warp_pattern_mode():
     """The warp-cooperative pattern mode writes and verifies every lane's whole
     block (512 bytes per instruction); counts and cleanliness as in the per-thread mode."""
