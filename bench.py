@@ -15,7 +15,7 @@ table (synthetic). One step = one launch over the whole grid.
   cpu_baseline     the oracle port of the reference's CPU backend on the host cores
 
 `--impl reference` times the reference's CPU implementation of the path (the
-oracle port) on the host cores instead.
+oracle port of its CPU backend, oracle/scatter_oracle.c) on the host cores instead.
 Multi-GPU: replicas only (each rank owns an independent heap).
 """
 from __future__ import annotations

@@ -219,8 +219,8 @@ mmc_status mmc_available_slots_noalloc(const mmc_device_handle* handle, size_t s
 mmc_status mmc_heap_error(mmc_heap* heap, void* stream, uint32_t* flags, int clear);
 
 /* Device event counters (MMC_STAT_*, MMC_STAT_COUNT values) into out; waits for
- * `stream`; clear != 0 zeroes them. The counters implement the survey-planned
- * allocator statistics (pages scanned, walk failures); they have no counterpart
+ * `stream`; clear != 0 zeroes them. The counters are allocator statistics
+ * (pages tried by walks, regions skipped, multi-page words scanned); they have no counterpart
  * in the reference and are maintained only in MMC_DEVICE_STATS builds. */
 mmc_status mmc_heap_stats(mmc_heap* heap, void* stream, unsigned long long* out, int clear);
 

@@ -7,7 +7,7 @@ parameter in turn is swept over its candidates with the others fixed, and the
 fastest value kept; two passes over all parameters. Every candidate is measured
 on a fresh heap as the median of `repeats` CUDA-event-timed runs of the batch
 (one graph launch each) after three warm-up runs, so geometries that degrade
-as the heap ages are judged aged. Candidates whose runs fail
+as the heap ages are measured aged. Candidates whose runs fail
 a job (a null allocation or a pattern error) are rejected.
 """
 from __future__ import annotations

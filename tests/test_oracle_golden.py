@@ -3,7 +3,7 @@
 Every fixture in tests/golden was produced by the unmodified reference
 (alpaka CPU-serial) via tests/golden/gen_golden.py. The oracle must reproduce
 each malloc offset, each getAvailableSlots value and each metadata snapshot
-bit for bit before it may judge the CUDA heap.
+bit for bit before it may check the CUDA heap.
 """
 import os
 
@@ -61,7 +61,7 @@ def test_oracle_matches_reference(name):
 
 
 def test_known_answers_literal():
-    """The survey's hand-checked values, independent of the fixture files."""
+    """Hand-checked known answers (64 MiB heap, sizes 16..8192), independent of the fixture files."""
     h = OracleHeap(REF_CONFIGS["p4k_ab8m_r16_w2"], 64 << 20)
     assert h.numpages == 16240
     assert h.available_slots(16) == 4124960
