@@ -594,21 +594,44 @@ def main():
     # ---- e2e: through the C ABI with host buffers ----
     e2e = None
     if not args.no_e2e:
-        evs2 = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+        # Each step's size table comes from pinned host memory and its counters go
+        # back to the host. The copy of step i+1's table runs on a copy stream
+        # while step i computes (two device buffers), as a pipelined caller would;
+        # the time is the whole span, from the first copy's start to the last
+        # step's counters on the host, L2 flushes between the steps included.
+        bufs = [d_sizes, torch.empty_like(d_sizes)]
+        copy_stream = torch.cuda.Stream()
+        ready = [torch.cuda.Event(), torch.cuda.Event()]
+        free = [torch.cuda.Event(), torch.cuda.Event()]
+        t_start, t_end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         torch.cuda.synchronize()
-        for e0, e1 in evs2:
+        t_start.record(stream)
+        copy_stream.wait_event(t_start)
+        with torch.cuda.stream(copy_stream):
+            bufs[0].copy_(h_sizes, non_blocking=True)
+            ready[0].record(copy_stream)
+        for i in range(args.steps):
+            b = i % 2
+            if i + 1 < args.steps:
+                nb = (i + 1) % 2
+                if i >= 1:
+                    copy_stream.wait_event(free[nb])  # step i-1 is done with that buffer
+                with torch.cuda.stream(copy_stream):
+                    bufs[nb].copy_(h_sizes, non_blocking=True)
+                    ready[nb].record(copy_stream)
             flush.zero_()
             stats.zero_()
-            e0.record(stream)
-            d_sizes.copy_(h_sizes, non_blocking=True)
-            step(d_sizes.data_ptr())
+            stream.wait_event(ready[b])
+            step(bufs[b].data_ptr())
+            free[b].record(stream)
             h_stats.copy_(stats, non_blocking=True)
-            e1.record(stream)
+        t_end.record(stream)
         torch.cuda.synchronize()
-        e2e_ms = max_over_ranks(sum(e0.elapsed_time(e1) for e0, e1 in evs2) / args.steps, dist, "cuda")
+        e2e_ms = max_over_ranks(t_start.elapsed_time(t_end) / args.steps, dist, "cuda")
         e2e = {"value": job_throughput(work["pairs"], world, e2e_ms), "unit": UNIT,
                "h2d_bytes_per_step": int(sizes_np.nbytes), "d2h_bytes_per_step": int(h_stats.numel() * 8),
-               "ms_per_step": e2e_ms}
+               "ms_per_step": e2e_ms,
+               "pipelining": "next step's H2D on a copy stream during the current step; L2 flushes inside the span"}
 
     if rank != 0:
         if dist:

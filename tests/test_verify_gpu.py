@@ -273,6 +273,29 @@ def test_stress_warp_pattern_reads_back_every_unit():
         assert st["checksum"] == _warp_pattern_checksum(sizes, seed, n)
 
 
+@pytest.mark.parametrize("size,xmalloc", [(256, True), (1024, True), (4096, True), (48, False), (2000, False)])
+def test_warp_uniform_sizes(size, xmalloc):
+    """Every lane of every warp asks for the same size, the case the same-size
+    group claim serves (one lane reserves and claims for the warp): patterns
+    intact, every pair counted, everything free afterwards; small sizes under
+    the Noop distribution keep the one-lane claim (hierarchical pages). Run
+    with the reference's exact-pagesize leak fixed (reference_quirks off):
+    with it, a 4096-byte block is never given back (the leak itself is
+    pinned by the golden fixtures)."""
+    import torch
+
+    from mallocmc_gb300.workloads import PATTERN_WARP, run_stress
+
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    cfg = HeapConfig(4096, 256 << 20, 16, 2, False, xmallocsimd=xmalloc, reference_quirks=False)
+    with gpu_allocator(cfg, 1 << 30) as alloc:
+        st = run_stress(alloc, sms * 2, 256, 10, size, size, 16, seed=21, write_pattern=PATTERN_WARP)
+        assert st["pairs"] == sms * 2 * 256 * 10, st
+        assert st["nulls"] == 0 and st["bad"] == 0, st
+        assert_all_free(alloc.snapshot())
+        assert alloc.error_flags() == 0
+
+
 def test_stress_full_size_steps_no_corruption():
     """The benchmark workload (8 GiB heap, SMs x 8 x 256 threads, 100 rounds of
     malloc / u64 pattern / verify / free) three times back to back: no block may
