@@ -118,8 +118,9 @@ def algorithmic_work(sizes: np.ndarray, pagesize: int = 4096):
 STRESS_DRAM_BYTES_PER_PAIR = 587.0
 # L2 atomic requests per pair counted by ncu (lts__t_requests_srcunit_tex_op_atom*
 # + op_red) in the same capture: below the reference algorithm's 4.72 because a
-# formatted page's chunk size is loaded instead of CAS'd.
-STRESS_NCU_ATOMICS_PER_PAIR = 4.04
+# formatted page's chunk size is loaded instead of CAS'd and same-size lanes
+# share one reservation.
+STRESS_NCU_ATOMICS_PER_PAIR = 4.01
 STRESS_TRAFFIC_NOTE = ("dram__bytes_read.sum + dram__bytes_write.sum per pair from an ncu capture of the same "
                        "kernel on a 2 GiB heap / 20 rounds, times the pairs of one launch")
 
