@@ -11,7 +11,6 @@ from __future__ import annotations
 
 import ctypes
 import time
-from collections import deque
 
 import numpy as np
 
@@ -81,20 +80,29 @@ class Server:
     def run(self, arrivals, lengths, seeds, batched: bool = True, realtime: bool = True, max_seconds: float = 60.0):
         """Serve the requests; returns a dict of per-request admit / done times
         (seconds from start), checksums, and loop counters. With realtime=False
-        every request is treated as arrived at the start (used by tests)."""
+        every request is treated as arrived at the start (used by tests).
+
+        Requests are admitted first come, first served: each tick admits the
+        longest prefix of the waiting requests whose expected chunks fit the
+        free-chunk count (less the chunks live requests will still take) and
+        for which a server slot is free. All per-tick work on the host is
+        vector operations over the slot table and the waiting range."""
         n = len(arrivals)
+        arrivals = np.asarray(arrivals)
+        lengths = np.asarray(lengths, dtype=np.int64)
+        seeds = np.asarray(seeds, dtype=np.int64)
         need = -(-lengths // ELEMS_PER_CHUNK)
         admit_t = np.full(n, np.nan)
         done_t = np.full(n, np.nan)
         checksum = np.zeros(n, dtype=np.uint64)
-        waiting = deque()
+        w_lo = 0  # requests w_lo .. nxt-1 have arrived and wait, in arrival order
         nxt = 0
         free_slots = list(range(self.nslots - 1, -1, -1))
         released = []  # slots whose release is in this tick's queue: reusable from the next tick on
         slot_req = np.full(self.nslots, -1, dtype=np.int64)
-        promised = 0  # chunks live requests will still take
         ticks = 0
         done = 0
+        q = self.queue
         # first tick: learn the free-slot count
         self.queue_len[0] = 0
         self.tick(batched)
@@ -103,42 +111,70 @@ class Server:
             now = time.perf_counter() - t0
             if now > max_seconds:
                 break
-            while nxt < n and (not realtime or arrivals[nxt] <= now):
-                waiting.append(nxt)
-                nxt += 1
-            cmds = 0
+            nxt = n if not realtime else int(np.searchsorted(arrivals, now, side="right"))
             free_slots.extend(released)
-            released = []
             # completions of the last tick
-            st = self.slots["state"]
-            for s in np.nonzero(st == L.MMC_SERVE_DONE)[0]:
-                r = slot_req[s]
-                if r >= 0:
-                    done_t[r] = now
-                    checksum[r] = self.slots["checksum"][s]
-                    done += 1
-                    slot_req[s] = -1
-                    released.append(int(s))
-                    self.queue[cmds] = (2, s, 0, 0, 0)
-                    cmds += 1
+            fin = np.flatnonzero((self.slots["state"] == L.MMC_SERVE_DONE) & (slot_req >= 0))
+            cmds = len(fin)
+            if cmds:
+                r = slot_req[fin]
+                done_t[r] = now
+                checksum[r] = self.slots["checksum"][fin]
+                done += cmds
+                slot_req[fin] = -1
+                q["kind"][:cmds] = 2
+                q["slot"][:cmds] = fin
+                q["id"][:cmds] = 0
+                q["final_len"][:cmds] = 0
+                q["seed"][:cmds] = 0
+            released = fin.tolist()
             live = slot_req >= 0
             promised = int((need[slot_req[live]] - self.slots["nchunks"][live]).sum()) if live.any() else 0
             available = int(self.free_chunks[0]) - promised
-            while waiting and free_slots and cmds < self.queue_cap:
-                r = waiting[0]
-                if need[r] > available:
-                    break
-                waiting.popleft()
-                s = free_slots.pop()
-                slot_req[s] = r
-                self.queue[cmds] = (1, s, r, int(lengths[r]), int(seeds[r]))
-                cmds += 1
-                available -= int(need[r])
-                admit_t[r] = now
+            k = min(nxt - w_lo, len(free_slots), self.queue_cap - cmds)
+            if k > 0:
+                k = int(np.searchsorted(np.cumsum(need[w_lo:w_lo + k]), available, side="right"))
+            if k > 0:
+                reqs = np.arange(w_lo, w_lo + k)
+                taken = np.asarray(free_slots[len(free_slots) - k:][::-1], dtype=np.int64)
+                del free_slots[len(free_slots) - k:]
+                slot_req[taken] = reqs
+                sl = slice(cmds, cmds + k)
+                q["kind"][sl] = 1
+                q["slot"][sl] = taken
+                q["id"][sl] = reqs
+                q["final_len"][sl] = lengths[reqs]
+                q["seed"][sl] = seeds[reqs].astype(np.uint64)
+                admit_t[reqs] = now
+                cmds += k
+                w_lo += k
             self.queue_len[0] = cmds
             self.tick(batched)
             ticks += 1
-            if not realtime and nxt >= n and not waiting and not (slot_req >= 0).any():
+            if not realtime and w_lo >= n and not (slot_req >= 0).any():
                 break
-        return {"admit": admit_t, "done": done_t, "checksum": checksum, "ticks": ticks,
-                "seconds": time.perf_counter() - t0, "completed": done}
+        seconds = time.perf_counter() - t0
+        self._drain(slot_req)
+        return {"admit": admit_t, "done": done_t, "checksum": checksum, "ticks": ticks, "seconds": seconds,
+                "completed": done}
+
+    def _drain(self, slot_req, max_seconds: float = 120.0):
+        """After a run that stopped with requests still growing: tick (one graph
+        launch each) without admissions until every live request has completed
+        and its slot is released, so the next run starts on an empty slot table
+        and a heap holding no chunks of this one. Nothing here is timed or
+        counted as served."""
+        q = self.queue
+        t0 = time.perf_counter()
+        pending = slot_req >= 0
+        while time.perf_counter() - t0 < max_seconds:
+            fin = np.flatnonzero((self.slots["state"] == L.MMC_SERVE_DONE) & pending)
+            k = len(fin)
+            q["kind"][:k] = 2
+            q["slot"][:k] = fin
+            pending[fin] = False
+            self.queue_len[0] = k
+            self.tick(True)
+            if not pending.any():
+                return
+        raise RuntimeError("serving loop did not drain its live requests")

@@ -54,3 +54,25 @@ def test_admission_waits_for_free_chunks():
         # never more chunks promised than the heap held: some requests had to wait
         assert np.nanmax(res["admit"]) > 0.0
         srv.close()
+
+
+def test_cut_short_run_drains_before_the_next():
+    """A run stopped by its time limit with requests still growing drains them
+    (their chunks freed, their slots released) before returning, so the next
+    run starts on an empty slot table: its checksums are right and the heap
+    ends clean."""
+    from mallocmc_gb300.serve import Server, expected_checksum, make_requests
+
+    arrivals, lengths, seeds = make_requests(64, rate=1e9, seed=9, median=16384, sigma=0.2)
+    want = np.array([expected_checksum(int(s), int(n)) for s, n in zip(seeds, lengths)], dtype=np.uint64)
+    with _server_heap() as alloc:
+        srv = Server(alloc, slots=64, max_chunks=128, step=16, queue_cap=128)
+        first = srv.run(arrivals, lengths, seeds, batched=True, realtime=False, max_seconds=0.002)
+        assert first["completed"] < len(arrivals)
+        assert not (srv.slots["state"] != 0).any()  # every slot free again
+        again = srv.run(arrivals, lengths, seeds, batched=True, realtime=False)
+        assert again["completed"] == len(arrivals)
+        assert np.array_equal(again["checksum"], want)
+        srv.close()
+        assert_all_free(alloc.snapshot(), pagesize=65536)
+        assert alloc.error_flags() == 0
