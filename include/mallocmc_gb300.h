@@ -407,9 +407,9 @@ typedef struct mmc_server mmc_server;
  * batched tick is captured into a CUDA graph here. */
 mmc_status mmc_serve_create(mmc_heap* heap, uint32_t slots, uint32_t max_chunks, uint32_t step, uint32_t queue_cap,
                             mmc_server** out);
-/* Pinned host views: the command queue and its length (written by the host
- * before a tick), the slot table and the free 16 KiB chunk count (as of the
- * end of the last tick). */
+/* Mapped pinned host views, which the tick's kernels read and write in place:
+ * the command queue and its length (written by the host before a tick), the
+ * slot table and the free 16 KiB chunk count (as of the end of the last tick). */
 mmc_status mmc_serve_queue(mmc_server* server, mmc_serve_cmd** queue, uint32_t** queue_len, mmc_serve_slot** slots,
                            unsigned** free_chunks);
 /* Run one tick and wait for it: batched != 0 replays the captured graph (all

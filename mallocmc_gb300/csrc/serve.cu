@@ -12,6 +12,12 @@
  * the requests that reach their length, and refreshes the free-slot count of
  * 16 KiB chunks that the host admits against. The per-request form launches
  * one grow kernel per live request instead.
+ *
+ * Host and device meet in mapped pinned memory: the kernels read the tick's
+ * commands where the host wrote them, write every slot they change through to
+ * the host's copy of the slot table, and the free-chunk count lands in host
+ * memory, so a tick has no copy steps (on GB300 the device reaches host
+ * memory over NVLink-C2C).
  */
 #include "mmc_internal.h"
 
@@ -47,20 +53,24 @@ struct mmc_server
     uint32_t queue_cap;
     mmc_serve_slot* d_slots;   /* slot table */
     void** d_chunks;           /* slots x max_chunks chunk pointers */
-    mmc_serve_cmd* d_queue;    /* this tick's admissions / releases */
-    uint32_t* d_queue_len;
-    mmc_serve_cmd* h_queue;    /* pinned staging of the queue */
-    uint32_t* h_queue_len;     /* pinned */
-    mmc_serve_slot* h_slots;   /* pinned copy of the slot table after each tick */
-    unsigned* d_free;          /* free 16 KiB slots after the tick */
-    unsigned* h_free;          /* pinned */
+    mmc_serve_cmd* h_queue;    /* this tick's admissions / releases (mapped pinned) */
+    uint32_t* h_queue_len;     /* mapped pinned */
+    mmc_serve_slot* h_slots;   /* the host's copy of the slot table, written through by the kernels */
+    unsigned* h_free;          /* free 16 KiB slots after the tick (mapped pinned) */
+    /* device addresses of the mapped pinned buffers above */
+    const mmc_serve_cmd* m_queue;
+    const uint32_t* m_queue_len;
+    mmc_serve_slot* m_slots;
+    unsigned* m_free;
     cudaStream_t stream;
     cudaGraphExec_t exec;
     cudaGraph_t graph;
 };
 
-/* Apply admissions (cmd.kind 1) and releases (cmd.kind 2). */
-__global__ void mmc_serve_apply(mmc_serve_slot* slots, const mmc_serve_cmd* q, const uint32_t* qlen)
+/* Apply admissions (cmd.kind 1) and releases (cmd.kind 2), read from the
+ * host's queue; each changed slot is also written to the host's table. */
+__global__ void mmc_serve_apply(mmc_serve_slot* slots, mmc_serve_slot* mirror, const mmc_serve_cmd* q,
+                                const uint32_t* qlen)
 {
     const uint32_t n = *qlen;
     for(uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
@@ -80,6 +90,7 @@ __global__ void mmc_serve_apply(mmc_serve_slot* slots, const mmc_serve_cmd* q, c
         }
         else if(c.kind == 2u)
             s.state = MMC_SERVE_FREE;
+        mirror[c.slot] = s;
     }
 }
 
@@ -151,10 +162,10 @@ __device__ __forceinline__ void grow_request(const mmc_device_handle& h, mmc_ser
     }
 }
 
-/* Batched tick: one warp per slot. */
+/* Batched tick: one warp per slot; each grown slot is written to the host's table. */
 __global__ void __launch_bounds__(256) mmc_serve_tick_kernel(mmc_device_handle h, mmc_serve_slot* slots,
-                                                             void** chunks, uint32_t nslots, uint32_t max_chunks,
-                                                             uint32_t step)
+                                                             mmc_serve_slot* mirror, void** chunks, uint32_t nslots,
+                                                             uint32_t max_chunks, uint32_t step)
 {
     const uint32_t warps = gridDim.x * (blockDim.x / 32u);
     for(uint32_t w = blockIdx.x * (blockDim.x / 32u) + threadIdx.x / 32u; w < nslots; w += warps)
@@ -162,16 +173,22 @@ __global__ void __launch_bounds__(256) mmc_serve_tick_kernel(mmc_device_handle h
         if(slots[w].state != MMC_SERVE_LIVE)
             continue;
         grow_request(h, slots[w], chunks + static_cast<uint64_t>(w) * max_chunks, max_chunks, step);
+        __syncwarp();
+        if((threadIdx.x & 31u) == 0u)
+            mirror[w] = slots[w];
     }
 }
 
 /* Per-request form: one warp, one slot. */
-__global__ void mmc_serve_one_kernel(mmc_device_handle h, mmc_serve_slot* slots, void** chunks, uint32_t slot,
-                                     uint32_t max_chunks, uint32_t step)
+__global__ void mmc_serve_one_kernel(mmc_device_handle h, mmc_serve_slot* slots, mmc_serve_slot* mirror,
+                                     void** chunks, uint32_t slot, uint32_t max_chunks, uint32_t step)
 {
     if(slots[slot].state != MMC_SERVE_LIVE)
         return;
     grow_request(h, slots[slot], chunks + static_cast<uint64_t>(slot) * max_chunks, max_chunks, step);
+    __syncwarp();
+    if(threadIdx.x == 0u)
+        mirror[slot] = slots[slot];
 }
 
 namespace
@@ -188,9 +205,6 @@ namespace
             cudaStreamDestroy(s->stream);
         cudaFree(s->d_slots);
         cudaFree(s->d_chunks);
-        cudaFree(s->d_queue);
-        cudaFree(s->d_queue_len);
-        cudaFree(s->d_free);
         cudaFreeHost(s->h_queue);
         cudaFreeHost(s->h_queue_len);
         cudaFreeHost(s->h_slots);
@@ -203,20 +217,16 @@ namespace
     mmc_status enqueue_tick(mmc_server* s, bool batched)
     {
         cudaStream_t st = s->stream;
-        cudaMemcpyAsync(s->d_queue_len, s->h_queue_len, sizeof(uint32_t), cudaMemcpyHostToDevice, st);
-        cudaMemcpyAsync(s->d_queue, s->h_queue, sizeof(mmc_serve_cmd) * s->queue_cap, cudaMemcpyHostToDevice, st);
-        mmc_serve_apply<<<8, 128, 0, st>>>(s->d_slots, s->d_queue, s->d_queue_len);
+        mmc_serve_apply<<<8, 128, 0, st>>>(s->d_slots, s->m_slots, s->m_queue, s->m_queue_len);
         if(batched)
         {
             const uint32_t blocks = (s->slots + 7u) / 8u;
-            mmc_serve_tick_kernel<<<blocks, 256, 0, st>>>(s->handle, s->d_slots, s->d_chunks, s->slots, s->max_chunks,
-                                                         s->step);
+            mmc_serve_tick_kernel<<<blocks, 256, 0, st>>>(s->handle, s->d_slots, s->m_slots, s->d_chunks, s->slots,
+                                                         s->max_chunks, s->step);
         }
-        mmc_status r = mmc_available_slots_async(s->heap, kChunkBytes, st, s->d_free);
+        mmc_status r = mmc_available_slots_async(s->heap, kChunkBytes, st, s->m_free);
         if(r != MMC_OK)
             return r;
-        cudaMemcpyAsync(s->h_slots, s->d_slots, sizeof(mmc_serve_slot) * s->slots, cudaMemcpyDeviceToHost, st);
-        cudaMemcpyAsync(s->h_free, s->d_free, sizeof(unsigned), cudaMemcpyDeviceToHost, st);
         return cuda_check(cudaGetLastError(), "serve tick");
     }
 } // namespace
@@ -245,19 +255,29 @@ mmc_status mmc_serve_create(mmc_heap* heap, uint32_t slots, uint32_t max_chunks,
     if(st == MMC_OK)
         st = cuda_check(cudaMalloc(&s->d_chunks, sizeof(void*) * static_cast<size_t>(slots) * max_chunks), "chunks");
     if(st == MMC_OK)
-        st = cuda_check(cudaMalloc(&s->d_queue, sizeof(mmc_serve_cmd) * queue_cap), "queue");
+        st = cuda_check(cudaHostAlloc(&s->h_queue, sizeof(mmc_serve_cmd) * queue_cap, cudaHostAllocMapped),
+                        "pinned queue");
     if(st == MMC_OK)
-        st = cuda_check(cudaMalloc(&s->d_queue_len, sizeof(uint32_t)), "queue length");
+        st = cuda_check(cudaHostAlloc(&s->h_queue_len, sizeof(uint32_t), cudaHostAllocMapped), "pinned queue length");
     if(st == MMC_OK)
-        st = cuda_check(cudaMalloc(&s->d_free, sizeof(unsigned)), "free count");
+        st = cuda_check(cudaHostAlloc(&s->h_slots, sizeof(mmc_serve_slot) * slots, cudaHostAllocMapped),
+                        "pinned slots");
     if(st == MMC_OK)
-        st = cuda_check(cudaMallocHost(&s->h_queue, sizeof(mmc_serve_cmd) * queue_cap), "pinned queue");
+        st = cuda_check(cudaHostAlloc(&s->h_free, sizeof(unsigned), cudaHostAllocMapped), "pinned free count");
     if(st == MMC_OK)
-        st = cuda_check(cudaMallocHost(&s->h_queue_len, sizeof(uint32_t)), "pinned queue length");
+        st = cuda_check(cudaHostGetDevicePointer(reinterpret_cast<void**>(const_cast<mmc_serve_cmd**>(&s->m_queue)),
+                                                 s->h_queue, 0),
+                        "mapped queue");
     if(st == MMC_OK)
-        st = cuda_check(cudaMallocHost(&s->h_slots, sizeof(mmc_serve_slot) * slots), "pinned slots");
+        st = cuda_check(cudaHostGetDevicePointer(reinterpret_cast<void**>(const_cast<uint32_t**>(&s->m_queue_len)),
+                                                 s->h_queue_len, 0),
+                        "mapped queue length");
     if(st == MMC_OK)
-        st = cuda_check(cudaMallocHost(&s->h_free, sizeof(unsigned)), "pinned free count");
+        st = cuda_check(cudaHostGetDevicePointer(reinterpret_cast<void**>(&s->m_slots), s->h_slots, 0),
+                        "mapped slots");
+    if(st == MMC_OK)
+        st = cuda_check(cudaHostGetDevicePointer(reinterpret_cast<void**>(&s->m_free), s->h_free, 0),
+                        "mapped free count");
     if(st == MMC_OK)
         st = cuda_check(cudaMemset(s->d_slots, 0, sizeof(mmc_serve_slot) * slots), "zero slots");
     if(st == MMC_OK)
@@ -319,24 +339,21 @@ mmc_status mmc_serve_tick(mmc_server* s, int batched)
         /* one grow launch per live request (from the host copy of the table),
          * around the same apply / count / download steps */
         cudaStream_t stream = s->stream;
-        cudaMemcpyAsync(s->d_queue_len, s->h_queue_len, sizeof(uint32_t), cudaMemcpyHostToDevice, stream);
-        cudaMemcpyAsync(s->d_queue, s->h_queue, sizeof(mmc_serve_cmd) * s->queue_cap, cudaMemcpyHostToDevice, stream);
-        mmc_serve_apply<<<8, 128, 0, stream>>>(s->d_slots, s->d_queue, s->d_queue_len);
-        for(uint32_t i = 0; i < *s->h_queue_len; ++i)
-            if(s->h_queue[i].kind == 1u)
-                s->h_slots[s->h_queue[i].slot].state = MMC_SERVE_LIVE;
+        /* which slots are live after this tick's admissions and releases, from
+         * the host's table and queue, before the apply kernel has run */
+        std::vector<uint8_t> live(s->slots, 0u);
         for(uint32_t w = 0; w < s->slots; ++w)
-            if(s->h_slots[w].state == MMC_SERVE_LIVE)
-                mmc_serve_one_kernel<<<1, 32, 0, stream>>>(s->handle, s->d_slots, s->d_chunks, w, s->max_chunks,
-                                                           s->step);
-        st = mmc_available_slots_async(s->heap, kChunkBytes, stream, s->d_free);
+            live[w] = s->h_slots[w].state == MMC_SERVE_LIVE;
+        for(uint32_t i = 0; i < *s->h_queue_len; ++i)
+            live[s->h_queue[i].slot] = s->h_queue[i].kind == 1u;
+        mmc_serve_apply<<<8, 128, 0, stream>>>(s->d_slots, s->m_slots, s->m_queue, s->m_queue_len);
+        for(uint32_t w = 0; w < s->slots; ++w)
+            if(live[w])
+                mmc_serve_one_kernel<<<1, 32, 0, stream>>>(s->handle, s->d_slots, s->m_slots, s->d_chunks, w,
+                                                           s->max_chunks, s->step);
+        st = mmc_available_slots_async(s->heap, kChunkBytes, stream, s->m_free);
         if(st == MMC_OK)
-        {
-            cudaMemcpyAsync(s->h_slots, s->d_slots, sizeof(mmc_serve_slot) * s->slots, cudaMemcpyDeviceToHost,
-                            stream);
-            cudaMemcpyAsync(s->h_free, s->d_free, sizeof(unsigned), cudaMemcpyDeviceToHost, stream);
             st = cuda_check(cudaGetLastError(), "per-request tick");
-        }
     }
     if(st == MMC_OK)
         st = cuda_check(cudaStreamSynchronize(s->stream), "tick");
