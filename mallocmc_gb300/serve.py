@@ -62,6 +62,9 @@ class Server:
         self.slots = np.ctypeslib.as_array(ctypes.cast(sl, ctypes.POINTER(ctypes.c_uint8)),
                                            shape=(slots * SLOT_DTYPE.itemsize,)).view(SLOT_DTYPE)
         self.free_chunks = np.ctypeslib.as_array(ctypes.cast(fr, ctypes.POINTER(ctypes.c_uint32)), shape=(1,))
+        # field views made once (a structured-array field lookup costs a microsecond a time)
+        self._state, self._nchunks, self._checksum = (self.slots[f] for f in ("state", "nchunks", "checksum"))
+        self._q = {f: self.queue[f] for f in ("kind", "slot", "id", "final_len", "seed")}
 
     def tick(self, batched: bool = True):
         L.check(L.lib().mmc_serve_tick(self._s, int(batched)), "serve_tick")
@@ -102,7 +105,8 @@ class Server:
         slot_req = np.full(self.nslots, -1, dtype=np.int64)
         ticks = 0
         done = 0
-        q = self.queue
+        q = self._q
+        state, nchunks, slot_checksum = self._state, self._nchunks, self._checksum
         # first tick: learn the free-slot count
         self.queue_len[0] = 0
         self.tick(batched)
@@ -114,12 +118,12 @@ class Server:
             nxt = n if not realtime else int(np.searchsorted(arrivals, now, side="right"))
             free_slots.extend(released)
             # completions of the last tick
-            fin = np.flatnonzero((self.slots["state"] == L.MMC_SERVE_DONE) & (slot_req >= 0))
+            fin = np.flatnonzero((state == L.MMC_SERVE_DONE) & (slot_req >= 0))
             cmds = len(fin)
             if cmds:
                 r = slot_req[fin]
                 done_t[r] = now
-                checksum[r] = self.slots["checksum"][fin]
+                checksum[r] = slot_checksum[fin]
                 done += cmds
                 slot_req[fin] = -1
                 q["kind"][:cmds] = 2
@@ -129,7 +133,7 @@ class Server:
                 q["seed"][:cmds] = 0
             released = fin.tolist()
             live = slot_req >= 0
-            promised = int((need[slot_req[live]] - self.slots["nchunks"][live]).sum()) if live.any() else 0
+            promised = int((need[slot_req[live]] - nchunks[live]).sum()) if live.any() else 0
             available = int(self.free_chunks[0]) - promised
             k = min(nxt - w_lo, len(free_slots), self.queue_cap - cmds)
             if k > 0:
@@ -164,11 +168,11 @@ class Server:
         and its slot is released, so the next run starts on an empty slot table
         and a heap holding no chunks of this one. Nothing here is timed or
         counted as served."""
-        q = self.queue
+        q = self._q
         t0 = time.perf_counter()
         pending = slot_req >= 0
         while time.perf_counter() - t0 < max_seconds:
-            fin = np.flatnonzero((self.slots["state"] == L.MMC_SERVE_DONE) & pending)
+            fin = np.flatnonzero((self._state == L.MMC_SERVE_DONE) & pending)
             k = len(fin)
             q["kind"][:k] = 2
             q["slot"][:k] = fin
