@@ -416,12 +416,13 @@ def fragmentation_column(torch, args, sms):
             "reference": ref, **runs}
 
 
-def cpu_port_run(heap_gib, threads_total, rounds, target_s, workers):
+def cpu_port_run(heap_gib, accessblock_mib, threads_total, rounds, target_s, workers):
     """The oracle port of the reference's CPU backend on `workers` host threads,
-    on a bounded sample (virtual threads x rounds) of the same workload."""
+    on a bounded sample (virtual threads x rounds) of the same workload and
+    heap geometry."""
     from oracle.oracle import HeapConfig, OracleHeap
 
-    cfg = HeapConfig(4096, 2 << 30, 16, 2, False)
+    cfg = HeapConfig(4096, accessblock_mib << 20, 16, 2, False)
     heap = OracleHeap(cfg, int(heap_gib * (1 << 30)))
     cal = heap.run_stress(4096, 4, SEED, 16, 1024, 16, workers)
     rate = cal["pairs"] / max(cal["seconds"], 1e-6)
@@ -484,11 +485,7 @@ def reference_arm(args):
         subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "liboracle.so"], check=True, capture_output=True)
     vals, samples = [], None
     for i in range(args.warmup + args.steps):
-        try:
-            r, vt = cpu_port_run(heap_gib, threads_total, args.rounds, per_step_s, workers)
-        except ValueError:
-            heap_gib = 1.0
-            r, vt = cpu_port_run(heap_gib, threads_total, args.rounds, per_step_s, workers)
+        r, vt = cpu_port_run(heap_gib, args.accessblock_mib, threads_total, args.rounds, per_step_s, workers)
         if i >= args.warmup:
             vals.append(r["pairs"] / r["seconds"])
             samples = (vt, r)
@@ -501,8 +498,8 @@ def reference_arm(args):
         "config": stress_config(args, 152, args.gpus),
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": workers, "kind": "port",
                          "sample": f"per step {r['steps']} x ({vt} virtual threads x {args.rounds} rounds) of the "
-                                   f"workload (alpaka CPU-backend semantics: warp size 1, smid = warpid = 0; the "
-                                   f"oracle's 2 GiB access blocks) on {workers} host threads, about {per_step_s:g} s"},
+                                   f"workload (alpaka CPU-backend semantics: warp size 1, smid = warpid = 0; same heap "
+                                   f"geometry) on {workers} host threads, about {per_step_s:g} s"},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "errors": {"nulls": r["nulls"], "pattern": r["bad"]},
     }
@@ -672,10 +669,7 @@ def main():
     cpu = None
     if not args.no_cpu_baseline:
         workers = os.cpu_count() or 1
-        try:
-            r, vt = cpu_port_run(args.heap_gib, nthreads, rounds, args.cpu_seconds, workers)
-        except ValueError:
-            r, vt = cpu_port_run(1.0, nthreads, rounds, args.cpu_seconds, workers)
+        r, vt = cpu_port_run(args.heap_gib, args.accessblock_mib, nthreads, rounds, args.cpu_seconds, workers)
         cpu = {"value": r["pairs"] / r["seconds"], "unit": UNIT, "cores": workers, "kind": "port",
                "sample": f"{r['steps']} x ({vt} virtual threads x {rounds} rounds) (alpaka CPU-backend semantics) "
                          f"on {workers} host threads, {r['seconds']:.1f} s"}
