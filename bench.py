@@ -1,17 +1,22 @@
 """Benchmark: device malloc+free throughput of the GB300 ScatterAlloc heap.
 
-Workload (the full-GPU uniform stress): an 8 GiB heap (pagesize 4096, the
-reference's default 2 GiB access blocks, regionsize 16, wastefactor 2,
-XMallocSIMD, ReturnNull, Shrink<16>); grid = SMs x 8 blocks x 256 threads;
-every thread runs 100 rounds of {malloc(size), write a u64 pattern, verify it,
-free}; sizes uniform in {16, 32, ..., 1024}, drawn from a seeded SplitMix64
-table (synthetic). One step = one launch over the whole grid.
+Headline workload (the full-GPU uniform stress): an 8 GiB heap (pagesize 4096,
+4 GiB access blocks by default, regionsize 16, wastefactor 2, XMallocSIMD,
+ReturnNull, Shrink<16>); grid = SMs x 8 blocks x 256 threads; every thread
+runs 100 rounds of {malloc(size), write a u64 pattern, verify it, free}; sizes
+uniform in {16, 32, ..., 1024}, drawn from a seeded SplitMix64 table
+(synthetic). One step = one launch over the whole grid.
 
-  value  pairs/s with the size table resident in HBM (kernel time, CUDA events)
-  e2e    pairs/s through the C ABI with host buffers: H2D of the step's size
-         table from pinned memory + kernel + D2H of the result counters
+  value            pairs/s with the size table resident in HBM (kernel time, CUDA events)
+  e2e              pairs/s through the C ABI with host buffers: H2D of each step's size
+                   table from pinned memory (pipelined on a copy stream) + kernel + D2H
+                   of the result counters, over the whole span
   roofline         HBM roofline of the stress kernel (payload + metadata bytes)
   atomic_roofline  L2 atomic ops/s against a measured atomicOr peak
+  oldmalloc        the same stress on CUDA's device heap (CreationPolicies::OldMalloc)
+  batched          uneven jobs in one graph-captured persistent launch vs one launch per job
+  serving          the continuous-batching request loop: p50/p99 latency and throughput
+  fragmentation    fill at out-of-memory against the oracle's serial run
   cpu_baseline     the oracle port of the reference's CPU backend on the host cores
 
 `--impl reference` times the reference's CPU implementation of the path (the

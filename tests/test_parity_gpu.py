@@ -142,16 +142,23 @@ def test_available_slots_fresh_heap(cfg_name, heap):
             assert alloc.getAvailableSlots(s) == oh.available_slots(s), s
 
 
-def test_available_slots_on_fragmented_state():
+@pytest.mark.parametrize("mix", ["mixed", "warp_uniform"])
+def test_available_slots_on_fragmented_state(mix):
     """A GPU-made, fragmented state (concurrent allocations with real thread
-    ids) counted by the GPU scan and by the oracle on the same snapshot."""
+    ids) counted by the GPU scan and by the oracle on the same snapshot; in
+    the warp-uniform case every warp's lanes ask for one size, so their chunks
+    come from same-size group claims."""
     from mallocmc_gb300.workloads import alloc_offsets
 
     cfg = REF_CONFIGS["p4k_ab8m_r16_w2"]
     heap = 64 << 20
     rng = np.random.default_rng(5)
     n = 16 * 256
-    sizes = rng.choice([16, 32, 48, 64, 128, 256, 600, 1000, 2048, 4096, 6000, 20000], size=n).astype(np.uint32)
+    choices = [16, 32, 48, 64, 128, 256, 600, 1000, 2048, 4096, 6000, 20000]
+    if mix == "mixed":
+        sizes = rng.choice(choices, size=n).astype(np.uint32)
+    else:
+        sizes = np.repeat(rng.choice([256, 600, 1000, 2048], size=n // 32), 32).astype(np.uint32)
     with gpu_allocator(cfg, heap) as alloc:
         alloc_offsets(alloc, 16, 256, sizes, 7)
         ptes, regions, masks, hdr = alloc.snapshot()
