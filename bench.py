@@ -14,7 +14,9 @@ uniform in {16, 32, ..., 1024}, drawn from a seeded SplitMix64 table
   roofline         HBM roofline of the stress kernel (payload + metadata bytes)
   atomic_roofline  L2 atomic ops/s against a measured atomicOr peak
   oldmalloc        the same stress on CUDA's device heap (CreationPolicies::OldMalloc)
-  batched          uneven jobs in one graph-captured persistent launch vs one launch per job
+  batched          uneven jobs in one graph-captured persistent launch vs one launch per job,
+                   with its own atomic roofline (the reference algorithm's atomics for
+                   the jobs' draws against the same measured peak)
   serving          the continuous-batching request loop: p50/p99 latency and throughput
   fragmentation    fill at out-of-memory against the oracle's serial run
   cpu_baseline     the oracle port of the reference's CPU backend on the host cores
@@ -76,7 +78,7 @@ def parse():
 def size_table(rounds: int, nthreads: int, seed: int = SEED) -> np.ndarray:
     """u16 [rounds, nthreads]: 16 * (1 + (mix64(seed, t, r) >> 32) % 64), the
     draw the stress kernel and the CPU port make when given no table."""
-    from oracle.oracle import mix64
+    from mallocmc_gb300.seeds import mix64
 
     t = np.arange(nthreads, dtype=np.uint64)
     out = np.empty((rounds, nthreads), dtype=np.uint16)
@@ -85,35 +87,70 @@ def size_table(rounds: int, nthreads: int, seed: int = SEED) -> np.ndarray:
     return out
 
 
-def algorithmic_work(sizes: np.ndarray, pagesize: int = 4096):
-    """Minimum global atomics and bytes per launch under the reference algorithm.
+def warp_atomics(w: np.ndarray, act: np.ndarray, pagesize: int) -> int:
+    """Minimum global atomics of malloc+free under the reference algorithm for
+    warp-synchronous rounds: w[..., 32] padded sizes, act[..., 32] the lanes
+    that take part in that round.
 
-    Per (warp, round): lanes with size < pagesize/32 coalesce (XMallocSIMD) when
-    there are at least two: one chunk of 16 + sum, malloc 3 atomics (CAS
-    chunksize, add count, or mask), free k refcount subtractions + 3 (hierarchical
-    chunk) or + 2; every other lane: 3 + 3 or 3 + 2. Hierarchical iff chunk <= (P-8)/33.
+    Lanes with size < pagesize/32 coalesce (XMallocSIMD) when there are at least
+    two: one chunk of 16 + sum, malloc 3 atomics (CAS chunksize, add count, or
+    mask), free k refcount subtractions + 3 (hierarchical chunk) or + 2; every
+    other lane: 3 + 3 or 3 + 2. Hierarchical iff chunk <= (P-8)/33."""
+    ht = (pagesize - 8) // 33
+    w = w.astype(np.int64)
+    co = act & (w < pagesize // 32)
+    k = co.sum(axis=-1)
+    csum = np.where(co, w, 0).sum(axis=-1)
+    grp = k >= 2
+    atom_g = np.where(grp, 3 + np.where(16 + csum <= ht, 3, 2) + k, 0)
+    single = act & ~(co & grp[..., None])
+    atom_s = np.where(single, 3 + np.where(np.maximum(w, 16) <= ht, 3, 2), 0)
+    return int(atom_g.sum() + atom_s.sum())
+
+
+def algorithmic_work(sizes: np.ndarray, pagesize: int = 4096):
+    """Minimum global atomics and bytes per launch of the stress under the
+    reference algorithm (warp_atomics over every (warp, round)).
     Bytes: payload written and read back (2 x size) + 4 B per atomic + 16 B of
     metadata reads per pair (chunksize on free, region counter, first-free-block,
     segment mask)."""
-    ht = (pagesize - 8) // 33
     s = sizes.astype(np.int64)
     R, T = s.shape
     w = s[:, : (T // 32) * 32].reshape(R, -1, 32)
-    co = w < pagesize // 32
-    k = co.sum(axis=2)
-    csum = np.where(co, w, 0).sum(axis=2)
-    grp = k >= 2
-    chunk_g = 16 + csum
-    atom_g = np.where(grp, 3 + np.where(chunk_g <= ht, 3, 2) + k, 0)
-    single = ~(co & grp[:, :, None])
-    c1 = np.maximum(w, 16)
-    atom_s = np.where(single, 3 + np.where(c1 <= ht, 3, 2), 0).sum(axis=2)
-    atomics = int(atom_g.sum() + atom_s.sum())
+    atomics = warp_atomics(w, np.ones(w.shape, dtype=bool), pagesize)
     pairs = int(s.size)
     payload = int(2 * s.sum())
     meta = 4 * atomics + 16 * pairs
     return {"pairs": pairs, "atomics": atomics, "atomics_per_pair": atomics / pairs, "payload_bytes": payload,
             "metadata_bytes": meta, "bytes": payload + meta}
+
+
+def batched_algorithmic_atomics(jobs, pagesize: int) -> dict:
+    """warp_atomics of the uneven-job workload: each job's threads form warps of
+    32 consecutive job threads; in cycle c the lanes whose cycle count exceeds c
+    take part with the size the kernels draw (geometric, float32 inverse CDF,
+    capped, padded to 16; csrc/batch.cu draw_size)."""
+    from mallocmc_gb300.seeds import mix64
+
+    atomics = pairs = payload = 0
+    for j in jobs:
+        T = (int(j.threads) + 31) // 32 * 32
+        t = np.arange(T, dtype=np.uint64)
+        span = np.uint64(j.max_cycles - j.min_cycles + 1)
+        cyc = j.min_cycles + ((mix64(j.seed, t, 0xC1C1E) >> np.uint64(32)) % span).astype(np.int64)
+        cyc[int(j.threads):] = 0
+        c = np.arange(j.max_cycles, dtype=np.uint64)[:, None]
+        m = mix64(j.seed, t[None, :], c)
+        u = ((m >> np.uint64(40)).astype(np.float32) + np.float32(0.5)) * np.float32(1.0 / 16777216.0)
+        q = np.float32(1.0) - np.float32(1.0) / np.float32(j.mean_size)
+        x = np.float32(1.0) + np.floor(np.log(u) / np.log(q))
+        x = np.minimum(x, np.float32(j.max_size))
+        sz = (x.astype(np.int64) + 15) & ~15
+        act = np.arange(j.max_cycles)[:, None] < cyc[None, :]
+        atomics += warp_atomics(sz.reshape(j.max_cycles, -1, 32), act.reshape(j.max_cycles, -1, 32), pagesize)
+        pairs += int(act.sum())
+        payload += int(np.where(act, sz, 0).sum())
+    return {"pairs": pairs, "atomics": atomics, "atomics_per_pair": atomics / pairs, "payload_bytes": payload}
 
 
 # DRAM bytes (read + written) per malloc+free pair of the stress kernel, from one
@@ -271,9 +308,11 @@ BATCH_TUNED = {"pagesize": 16384, "regionsize": 32, "hashingK": 7919, "hashingDi
                "accessblock_fraction": 1, "blocks_per_sm": 8}
 
 
-def batched_column(torch, args, sms):
+def batched_column(torch, args, sms, atom_peak=None):
     """512 uneven jobs on one 16 GiB heap: one persistent graph-captured launch
-    against one plain launch per job (same allocations, checked job by job)."""
+    against one plain launch per job (same allocations, checked job by job).
+    With atom_peak (measured L2 atomics/s), each form's algorithmic atomics per
+    second (batched_algorithmic_atomics) against it."""
     from mallocmc_gb300 import AlignmentPolicies, Allocator, CreationPolicies, DistributionPolicies
     from mallocmc_gb300.autotune import TuneConfig, _accessblock, autotune
     from mallocmc_gb300.batch import Batch, expected_pairs, make_jobs
@@ -320,16 +359,28 @@ def batched_column(torch, args, sms):
         return out
 
     tuned = run(cfg, "tuned")
-    ref = run(TuneConfig(), "reference defaults")
+    ref_cfg = TuneConfig()
+    ref = run(ref_cfg, "reference defaults")
     pairs = int(want.sum())
+
+    def atomic_roofline(c, ms):
+        if atom_peak is None:
+            return None
+        w = batched_algorithmic_atomics(jobs, c.pagesize)
+        ach = w["atomics"] / (ms * 1e-3)
+        return {"bound": "l2_atomic", "achieved": ach / 1e9, "peak": atom_peak / 1e9, "unit": "Gatomic/s",
+                "frac": ach / atom_peak, "atomics_per_pair": w["atomics_per_pair"], "form": "graph"}
+
     res = {"workload": "512 jobs on a 16 GiB heap, threads log-uniform in [32, 65536], sizes geometric "
                        "(mean 64 B, cap 4 KiB, padded to 16), 1-16 cycles per thread",
            "pairs_per_step": pairs, "threads": int(sum(j.threads for j in jobs)),
            "graph_value": pairs / (tuned["graph"] * 1e-3), "plain_value": pairs / (tuned["plain"] * 1e-3),
            "speedup_graph_vs_plain": tuned["plain"] / tuned["graph"], "unit": UNIT,
            "ms": tuned, "tuned_config": dict(cfg.__dict__),
+           "atomic_roofline": atomic_roofline(cfg, tuned["graph"]),
            "reference_defaults": {"ms": ref, "speedup_graph_vs_plain": ref["plain"] / ref["graph"],
-                                  "graph_value": pairs / (ref["graph"] * 1e-3)}}
+                                  "graph_value": pairs / (ref["graph"] * 1e-3),
+                                  "atomic_roofline": atomic_roofline(ref_cfg, ref["graph"])}}
     if tune_trace is not None:
         res["autotune_trace"] = tune_trace
     return res
@@ -651,6 +702,7 @@ def main():
                 "algorithmic_bytes_per_launch": work["bytes"], "payload_bytes_per_launch": work["payload_bytes"],
                 "metadata_bytes_per_launch": work["metadata_bytes"], "kernel": "mmc_stress_kernel"}
     atomic = None
+    pk = None
     if not args.no_peak:
         pk = atomic_peak(torch, sms)
         ach = work["atomics"] / kernel_s
@@ -661,7 +713,7 @@ def main():
                   "peaks_measured_gops": {k: v / 1e9 for k, v in pk.items()}}
     batched = None
     if not args.no_batched:
-        batched = batched_column(torch, args, sms)
+        batched = batched_column(torch, args, sms, pk["atom_l2_32MiB"] if pk else None)
     serving = None
     if not args.no_serve:
         serving = serving_column(torch, args)

@@ -8,10 +8,12 @@
  *
  * Two forms of the same work:
  *   plain       one kernel launch per job (grid = ceil(threads / 256))
- *   persistent  one launch of a fixed grid whose blocks take work items
- *               (256-thread slices of any job) from a device counter until the
- *               batch is done; the counter reset and the launch are captured
- *               once into a CUDA graph and replayed per run.
+ *   persistent  one launch of a fixed grid whose lanes take job threads
+ *               from a device counter until the batch is done: a lane whose
+ *               thread has run its last cycle takes the next one at once, so
+ *               no warp idles while its slowest lane finishes (cycle counts
+ *               differ by up to 16x within a warp). The counter reset and the
+ *               launch are captured once into a CUDA graph and replayed per run.
  * Per-job counters {pairs, nulls, pattern errors, checksum} make the forms
  * comparable job by job.
  */
@@ -36,7 +38,7 @@ struct mmc_batch
     uint32_t threads_per_block;
     std::vector<mmc_job> host_jobs;
     mmc_job* jobs;              /* device copy, item_begin filled */
-    unsigned* counter;          /* work-item counter of the persistent form */
+    unsigned long long* counter; /* job-thread counter of the persistent form */
     unsigned long long* stats;  /* njobs x 4 */
     cudaGraph_t graph;
     cudaGraphExec_t exec;
@@ -138,42 +140,106 @@ __global__ void __launch_bounds__(256) mmc_job_kernel(mmc_device_handle h, const
     flush_stats(stats + 4ull * job, pairs, nulls, bad, csum);
 }
 
-/* Persistent form: blocks take 256-thread work items from *counter. */
+/* Persistent form. Job threads are numbered in work-item space: job i owns
+ * slots [256 * item_begin_i, 256 * item_begin_i + threads_i); the slots up to
+ * the next job's first item are padding and are skipped. Every lane runs one
+ * job thread at a time, one cycle per pass of the loop; lanes that need a
+ * thread take consecutive slots with one atomicAdd per warp. A lane's counters
+ * are flushed to its job's row when it leaves a thread. */
 __global__ void __launch_bounds__(256) mmc_batch_kernel(mmc_device_handle h, const mmc_job* jobs, uint32_t njobs,
-                                                        uint32_t total_items, unsigned* counter,
+                                                        unsigned long long total_slots, unsigned long long* counter,
                                                         unsigned long long* stats)
 {
-    __shared__ uint32_t s_item, s_job;
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t lanes_below = (1u << lane) - 1u;
+    uint32_t job = 0, jt = 0, cycles = 0, c = 0;
+    uint64_t seed = 0;
+    mmc_job j{};
+    bool done = false;
+    unsigned long long pairs = 0, nulls = 0, bad = 0, csum = 0;
     for(;;)
     {
-        if(threadIdx.x == 0)
+        bool need = !done && c == cycles;
+        unsigned needm = __ballot_sync(0xFFFFFFFFu, need);
+        while(needm != 0u)
         {
-            const uint32_t item = atomicAdd(counter, 1u);
-            uint32_t lo = 0, hi = njobs; /* last job whose first item <= item */
-            if(item < total_items)
-                while(hi - lo > 1u)
+            const int leader = __ffs(static_cast<int>(needm)) - 1;
+            unsigned long long base = 0;
+            if(static_cast<int>(lane) == leader)
+                base = atomicAdd(counter, static_cast<unsigned long long>(__popc(needm)));
+            base = __shfl_sync(0xFFFFFFFFu, base, leader);
+            if(need)
+            {
+                if(cycles != 0u)
                 {
-                    const uint32_t mid = (lo + hi) / 2u;
-                    if(jobs[mid].item_begin <= item)
-                        lo = mid;
-                    else
-                        hi = mid;
+                    unsigned long long* s = stats + 4ull * job;
+                    atomicAdd(&s[0], pairs);
+                    if(nulls)
+                        atomicAdd(&s[1], nulls);
+                    if(bad)
+                        atomicAdd(&s[2], bad);
+                    atomicXor(&s[3], csum);
+                    pairs = nulls = bad = csum = 0;
+                    cycles = c = 0;
                 }
-            s_item = item;
-            s_job = lo;
+                const unsigned long long slot = base + static_cast<unsigned>(__popc(needm & lanes_below));
+                if(slot >= total_slots)
+                {
+                    done = true;
+                    need = false;
+                }
+                else
+                {
+                    const uint32_t item = static_cast<uint32_t>(slot / kItemThreads);
+                    uint32_t lo = 0, hi = njobs; /* last job whose first item <= item */
+                    while(hi - lo > 1u)
+                    {
+                        const uint32_t mid = (lo + hi) / 2u;
+                        if(jobs[mid].item_begin <= item)
+                            lo = mid;
+                        else
+                            hi = mid;
+                    }
+                    job = lo;
+                    j = jobs[job];
+                    jt = static_cast<uint32_t>(slot - static_cast<unsigned long long>(j.item_begin) * kItemThreads);
+                    if(jt < j.threads)
+                    {
+                        const uint32_t span = j.max_cycles - j.min_cycles + 1u;
+                        cycles = j.min_cycles + static_cast<uint32_t>(mix64(j.seed, jt, 0xC1C1Eull) >> 32) % span;
+                        seed = j.seed;
+                        need = cycles == 0u; /* a thread with no cycles is done at once */
+                    }
+                }
+            }
+            needm = __ballot_sync(0xFFFFFFFFu, need);
         }
-        __syncthreads();
-        const uint32_t item = s_item;
-        const uint32_t job = s_job;
-        __syncthreads();
-        if(item >= total_items)
-            return;
-        const mmc_job j = jobs[job];
-        const uint32_t jt = (item - j.item_begin) * kItemThreads + threadIdx.x;
-        unsigned long long pairs = 0, nulls = 0, bad = 0, csum = 0;
-        if(jt < j.threads)
-            run_job_thread(h, j, jt, pairs, nulls, bad, csum);
-        flush_stats(stats + 4ull * job, pairs, nulls, bad, csum);
+        if(__all_sync(0xFFFFFFFFu, done))
+            break;
+        if(!done)
+        {
+            const uint64_t m = mix64(seed, jt, c);
+            const uint32_t bytes = draw_size(j, m);
+            char* ptr = static_cast<char*>(dv::malloc<dv::GpuIds>(h, bytes));
+            if(ptr == nullptr)
+                ++nulls;
+            else
+            {
+                ulonglong2* q = reinterpret_cast<ulonglong2*>(ptr);
+                const uint32_t n16 = bytes / 16u;
+                for(uint32_t i = 0; i < n16; ++i)
+                    q[i] = make_ulonglong2(m + 2u * i, m + 2u * i + 1u);
+                for(uint32_t i = 0; i < n16; ++i)
+                {
+                    const ulonglong2 v = q[i];
+                    bad += (v.x != m + 2u * i) + (v.y != m + 2u * i + 1u);
+                    csum += v.x ^ v.y;
+                }
+                dv::free<dv::GpuIds>(h, ptr);
+                ++pairs;
+            }
+            ++c;
+        }
     }
 }
 
@@ -200,9 +266,10 @@ namespace
 
     void launch_persistent(mmc_batch* b, cudaStream_t s)
     {
-        cudaMemsetAsync(b->counter, 0, sizeof(unsigned), s);
-        mmc_batch_kernel<<<b->blocks, kItemThreads, 0, s>>>(b->handle, b->jobs, b->njobs, b->total_items, b->counter,
-                                                            b->stats);
+        cudaMemsetAsync(b->counter, 0, sizeof(unsigned long long), s);
+        mmc_batch_kernel<<<b->blocks, kItemThreads, 0, s>>>(b->handle, b->jobs, b->njobs,
+                                                            static_cast<unsigned long long>(b->total_items) * kItemThreads,
+                                                            b->counter, b->stats);
     }
 } // namespace
 
@@ -244,7 +311,7 @@ mmc_status mmc_batch_create(mmc_heap* heap, const mmc_job* jobs, uint32_t njobs,
     cudaStream_t s = as_stream(stream);
     mmc_status st = cuda_check(cudaMalloc(&b->jobs, sizeof(mmc_job) * njobs), "cudaMalloc jobs");
     if(st == MMC_OK)
-        st = cuda_check(cudaMalloc(&b->counter, sizeof(unsigned)), "cudaMalloc counter");
+        st = cuda_check(cudaMalloc(&b->counter, sizeof(unsigned long long)), "cudaMalloc counter");
     if(st == MMC_OK)
         st = cuda_check(cudaMalloc(&b->stats, sizeof(unsigned long long) * 4ull * njobs), "cudaMalloc stats");
     if(st == MMC_OK)

@@ -51,3 +51,27 @@ def test_batch_checksums_equal_across_forms():
         batched = b.stats()
         b.close()
         assert np.array_equal(plain, batched)
+
+
+def test_batch_jobs_of_one_thread_and_zero_cycles():
+    """Jobs of a single thread, thread counts off the 256-thread item grid, and
+    threads with no cycles at all: the persistent form skips padding slots and
+    empty threads and still matches the plain launches job by job."""
+    from mallocmc_gb300.batch import Batch, expected_pairs, make_jobs
+
+    jobs = make_jobs(njobs=40, seed=13, tmin=1, tmax=700, min_cycles=0, max_cycles=3)
+    jobs[0].threads = 1
+    jobs[7].threads = 257
+    want = expected_pairs(jobs)
+    cfg = HeapConfig(4096, 256 << 20, 16, 2, False)
+    with gpu_allocator(cfg, 1 << 30) as alloc:
+        b = Batch(alloc, jobs, persistent_blocks=152, use_graph=True)
+        b.run_plain()
+        plain = b.stats()
+        b.run()
+        batched = b.stats()
+        b.close()
+        assert np.array_equal(plain[:, 0].astype(np.int64), want)
+        assert np.array_equal(plain, batched)
+        assert_all_free(alloc.snapshot())
+        assert alloc.error_flags() == 0
