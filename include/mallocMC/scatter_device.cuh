@@ -1036,10 +1036,25 @@ namespace mmc
             const u32 inblockoffset = inpage_offset - block * chunksize;
             if(inblockoffset != 0u)
             {
-                /* XMallocSIMD sub-allocation: the lane count lives at the chunk head */
+                /* XMallocSIMD sub-allocation: the lane count lives at the chunk head.
+                 * Lanes freeing parts of the same chunk together subtract as one
+                 * (the lowest of them, after a __syncwarp that orders every
+                 * peer's accesses to its part before the decrement); whoever
+                 * takes the count to zero frees the chunk, as each lane's own
+                 * decrement would. */
                 u32* counter = reinterpret_cast<u32*>(page_data(h, page) + block * chunksize);
-                const u32 old = atomicSub(counter, 1u);
-                if(old != 1u)
+                u32 sub = 1u;
+                if constexpr(Ids::warpSize > 1u)
+                {
+                    const u32 peers
+                        = __match_any_sync(__activemask(), reinterpret_cast<unsigned long long>(counter));
+                    __syncwarp(peers);
+                    if(Ids::laneid() != static_cast<u32>(__ffs(static_cast<int>(peers))) - 1u)
+                        return;
+                    sub = static_cast<u32>(__popc(peers));
+                }
+                const u32 old = atomicSub(counter, sub);
+                if(old != sub)
                     return;
                 mem = counter;
             }
