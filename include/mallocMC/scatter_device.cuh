@@ -1131,7 +1131,13 @@ namespace mmc
             void* mem = create<Ids>(h, req);
             mem = handle_oom(h, mem, req);
             if(coalescible && lane == leader && mem != nullptr)
+            {
                 st_rlx(static_cast<u32*>(mem), threadcount);
+                /* The count's sector is usually cold, and the store leaves it
+                 * partly valid in L2: the frees' atomics on it would wait for
+                 * the DRAM fill. Fetch it now, while the lanes use their parts. */
+                asm volatile("prefetch.global.L2 [%0];" ::"l"(mem));
+            }
             /* The lane count must be seen by every later free of a sub-allocation
              * (device-scope atomicSubs on this word). The warp barrier orders
              * the leader's store before every lane's accesses after it, the

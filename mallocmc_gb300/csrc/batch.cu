@@ -39,6 +39,7 @@ struct mmc_batch
     std::vector<mmc_job> host_jobs;
     mmc_job* jobs;              /* device copy, item_begin filled */
     unsigned long long* counter; /* job-thread counter of the persistent form */
+    bool shared_rows;            /* per-block pair/checksum columns fit shared memory and u32 */
     unsigned long long* stats;  /* njobs x 4 */
     cudaGraph_t graph;
     cudaGraphExec_t exec;
@@ -48,6 +49,9 @@ struct mmc_batch
 namespace
 {
     constexpr uint32_t kItemThreads = 256;
+    /* per-block pair and checksum columns in shared memory up to 32 KiB
+     * (2730 jobs); larger batches flush to the global table directly */
+    constexpr size_t kSharedRowsMax = 32u << 10;
 
     __host__ __device__ __forceinline__ uint64_t mix64(uint64_t seed, uint64_t a, uint64_t b)
     {
@@ -145,11 +149,28 @@ __global__ void __launch_bounds__(256) mmc_job_kernel(mmc_device_handle h, const
  * the next job's first item are padding and are skipped. Every lane runs one
  * job thread at a time, one cycle per pass of the loop; lanes that need a
  * thread take consecutive slots with one atomicAdd per warp. A lane's counters
- * are flushed to its job's row when it leaves a thread. */
+ * are flushed to its job's row when it leaves a thread. With SHARED_ROWS the
+ * pairs and the checksum (the words every thread adds to) go to the block's
+ * copy of those two columns in shared memory (12 B per job), which the block
+ * adds to the global table once at its end; without, and for the rare null and
+ * pattern-error counts, straight to the global table. (One thread's flush to
+ * L2 is two atomics, more than its share of the allocations' atomics.) */
+template<bool SHARED_ROWS>
 __global__ void __launch_bounds__(256) mmc_batch_kernel(mmc_device_handle h, const mmc_job* jobs, uint32_t njobs,
                                                         unsigned long long total_slots, unsigned long long* counter,
                                                         unsigned long long* stats)
 {
+    extern __shared__ unsigned long long s_csum[]; /* njobs checksums, then njobs u32 pair counts */
+    uint32_t* s_pairs = reinterpret_cast<uint32_t*>(s_csum + njobs);
+    if constexpr(SHARED_ROWS)
+    {
+        for(uint32_t i = threadIdx.x; i < njobs; i += blockDim.x)
+        {
+            s_csum[i] = 0ull;
+            s_pairs[i] = 0u;
+        }
+        __syncthreads();
+    }
     const uint32_t lane = threadIdx.x & 31u;
     const uint32_t lanes_below = (1u << lane) - 1u;
     uint32_t job = 0, jt = 0, cycles = 0, c = 0;
@@ -173,12 +194,20 @@ __global__ void __launch_bounds__(256) mmc_batch_kernel(mmc_device_handle h, con
                 if(cycles != 0u)
                 {
                     unsigned long long* s = stats + 4ull * job;
-                    atomicAdd(&s[0], pairs);
+                    if constexpr(SHARED_ROWS)
+                    {
+                        atomicAdd(&s_pairs[job], static_cast<uint32_t>(pairs));
+                        atomicXor(&s_csum[job], csum);
+                    }
+                    else
+                    {
+                        atomicAdd(&s[0], pairs);
+                        atomicXor(&s[3], csum);
+                    }
                     if(nulls)
                         atomicAdd(&s[1], nulls);
                     if(bad)
                         atomicAdd(&s[2], bad);
-                    atomicXor(&s[3], csum);
                     pairs = nulls = bad = csum = 0;
                     cycles = c = 0;
                 }
@@ -241,6 +270,17 @@ __global__ void __launch_bounds__(256) mmc_batch_kernel(mmc_device_handle h, con
             ++c;
         }
     }
+    if constexpr(SHARED_ROWS)
+    {
+        __syncthreads();
+        for(uint32_t i = threadIdx.x; i < njobs; i += blockDim.x)
+        {
+            if(s_pairs[i] != 0u)
+                atomicAdd(&stats[4ull * i], static_cast<unsigned long long>(s_pairs[i]));
+            if(s_csum[i] != 0ull)
+                atomicXor(&stats[4ull * i + 3u], s_csum[i]);
+        }
+    }
 }
 
 namespace
@@ -267,9 +307,14 @@ namespace
     void launch_persistent(mmc_batch* b, cudaStream_t s)
     {
         cudaMemsetAsync(b->counter, 0, sizeof(unsigned long long), s);
-        mmc_batch_kernel<<<b->blocks, kItemThreads, 0, s>>>(b->handle, b->jobs, b->njobs,
-                                                            static_cast<unsigned long long>(b->total_items) * kItemThreads,
-                                                            b->counter, b->stats);
+        const unsigned long long slots = static_cast<unsigned long long>(b->total_items) * kItemThreads;
+        const size_t rows_bytes = (sizeof(unsigned long long) + sizeof(uint32_t)) * b->njobs;
+        if(b->shared_rows)
+            mmc_batch_kernel<true><<<b->blocks, kItemThreads, rows_bytes, s>>>(b->handle, b->jobs, b->njobs, slots,
+                                                                                b->counter, b->stats);
+        else
+            mmc_batch_kernel<false><<<b->blocks, kItemThreads, 0, s>>>(b->handle, b->jobs, b->njobs, slots,
+                                                                        b->counter, b->stats);
     }
 } // namespace
 
@@ -307,6 +352,10 @@ mmc_status mmc_batch_create(mmc_heap* heap, const mmc_job* jobs, uint32_t njobs,
         return fail(MMC_ERR_ARG, "batch too large");
     }
     b->total_items = static_cast<uint32_t>(items);
+    b->shared_rows = (sizeof(unsigned long long) + sizeof(uint32_t)) * njobs <= kSharedRowsMax;
+    for(const auto& j : b->host_jobs)
+        if(static_cast<uint64_t>(j.threads) * j.max_cycles > 0xFFFFFFFFull)
+            b->shared_rows = false; /* a block's pair count of the job could pass 32 bits */
     b->blocks = persistent_blocks ? persistent_blocks : scan_grid(b->device) * 2u;
     cudaStream_t s = as_stream(stream);
     mmc_status st = cuda_check(cudaMalloc(&b->jobs, sizeof(mmc_job) * njobs), "cudaMalloc jobs");

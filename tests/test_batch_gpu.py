@@ -75,3 +75,24 @@ def test_batch_jobs_of_one_thread_and_zero_cycles():
         assert np.array_equal(plain, batched)
         assert_all_free(alloc.snapshot())
         assert alloc.error_flags() == 0
+
+
+def test_batch_beyond_the_shared_job_table():
+    """3000 jobs do not fit the per-block job columns in shared memory: the
+    persistent form then flushes every thread's counters to the global table
+    and still matches the plain launches job by job."""
+    from mallocmc_gb300.batch import Batch, expected_pairs, make_jobs
+
+    jobs = make_jobs(njobs=3000, seed=14, tmin=1, tmax=64, max_cycles=4)
+    want = expected_pairs(jobs)
+    cfg = HeapConfig(4096, 256 << 20, 16, 2, False)
+    with gpu_allocator(cfg, 1 << 30) as alloc:
+        b = Batch(alloc, jobs, persistent_blocks=304, use_graph=True)
+        b.run_plain()
+        plain = b.stats()
+        b.run()
+        batched = b.stats()
+        b.close()
+        assert np.array_equal(plain[:, 0].astype(np.int64), want)
+        assert np.array_equal(plain, batched)
+        assert alloc.error_flags() == 0
