@@ -2,9 +2,13 @@
 access block size, regionsize), the page-hash primes (hashingK, hashingDistMP)
 and the persistent grid size for a given job table.
 
-The search is coordinate descent: starting from the reference defaults, each
-parameter in turn is swept over its candidates with the others fixed, and the
-fastest value kept; two passes over all parameters. Every candidate is measured
+The search is a coordinate descent per pagesize: the pagesize changes the
+heap most (which sizes coalesce, which pages are hierarchical), so one descent
+that sweeps it with the rest at the reference defaults settles in the wrong
+basin. For each candidate pagesize, from the reference defaults, every other
+parameter in turn is swept over its candidates with the rest fixed and the
+fastest value kept, two passes over all of them; the fastest of the per-
+pagesize results wins. Every candidate is measured
 on a fresh heap as the median of `repeats` CUDA-event-timed runs of the batch
 (one graph launch each) after three warm-up runs, so geometries that degrade
 as the heap ages are measured aged. Candidates whose runs fail
@@ -92,19 +96,20 @@ def measure(cfg: TuneConfig, jobs, heap_bytes: int, device: int, sms: int, expec
 
 
 def autotune(jobs, heap_bytes: int, device: int = 0, passes: int = 2, repeats: int = 3, expected=None,
-             log=None):
-    """Coordinate descent over TuneConfig; returns (best config, best ms, trace)."""
-    import torch
+             log=None, starts=None, sms=None):
+    """Coordinate descent over TuneConfig with the pagesize held at each start's
+    (default starts: the reference defaults at every candidate pagesize);
+    returns (best config, best ms, trace)."""
+    if sms is None:
+        import torch
 
-    sms = torch.cuda.get_device_properties(device).multi_processor_count
+        sms = torch.cuda.get_device_properties(device).multi_processor_count
     space = {
-        "pagesize": PAGESIZES,
         "regionsize": REGIONSIZES,
         "hash": HASH_PRIMES,
         "accessblock_fraction": ACCESSBLOCK_FRACTIONS,
         "blocks_per_sm": BLOCKS_PER_SM,
     }
-    best = TuneConfig()
     cache = {}
 
     def score(c):
@@ -114,16 +119,28 @@ def autotune(jobs, heap_bytes: int, device: int = 0, passes: int = 2, repeats: i
                 log(asdict(c), cache[c])
         return cache[c]
 
-    best_ms = score(best)
-    for _ in range(passes):
-        for name, values in space.items():
-            for v in values:
-                if name == "hash":
-                    cand = replace(best, hashingK=v[0], hashingDistMP=v[1])
-                else:
-                    cand = replace(best, **{name: v})
-                ms = score(cand)
-                if ms is not None and (best_ms is None or ms < best_ms):
-                    best, best_ms = cand, ms
+    def descend(best):
+        best_ms = score(best)
+        for _ in range(passes):
+            for name, values in space.items():
+                for v in values:
+                    if name == "hash":
+                        cand = replace(best, hashingK=v[0], hashingDistMP=v[1])
+                    else:
+                        cand = replace(best, **{name: v})
+                    ms = score(cand)
+                    if ms is not None and (best_ms is None or ms < best_ms):
+                        best, best_ms = cand, ms
+        return best, best_ms
+
+    if starts is None:
+        starts = [replace(TuneConfig(), pagesize=p) for p in PAGESIZES]
+    best, best_ms = None, None
+    for start in starts:
+        c, ms = descend(start)
+        if ms is not None and (best_ms is None or ms < best_ms):
+            best, best_ms = c, ms
+    if best is None:
+        best = TuneConfig()
     trace = [{"config": asdict(c), "ms": ms} for c, ms in cache.items()]
     return best, best_ms, trace
