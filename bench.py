@@ -304,10 +304,14 @@ def oldmalloc_column(torch, stream, heap_bytes, blocks, tpb, rounds, d_sizes, fl
 
 # The batched workload's geometry as chosen by mallocmc_gb300.autotune (a coordinate
 # descent over regionsize, hash primes, access block and grid per pagesize) on a
-# GB300 (`bench.py --autotune` re-runs it): 2.33 ms per aged graph launch; the
-# runners-up within 1 % differ in the hash primes or the grid.
-BATCH_TUNED = {"pagesize": 16384, "regionsize": 32, "hashingK": 38183, "hashingDistMP": 17497,
-               "accessblock_fraction": 1, "blocks_per_sm": 16}
+# GB300 (`bench.py --autotune` re-runs it). Its two best points, 16 KiB pages with
+# the (38183, 17497) or the (7919, 101) hash primes, time within 0.3 % of each
+# other (2.33-2.34 ms per graph launch, flat over 60 launches on the 16 GiB heap);
+# on an 8 GiB heap the first collapses after about 45 launches (pages of the
+# right chunk size run out) while the second stays near 2.5 ms, so this is the
+# second.
+BATCH_TUNED = {"pagesize": 16384, "regionsize": 32, "hashingK": 7919, "hashingDistMP": 101,
+               "accessblock_fraction": 1, "blocks_per_sm": 8}
 
 
 def batched_column(torch, args, sms, atom_peak=None):

@@ -9,10 +9,11 @@ basin. For each candidate pagesize, from the reference defaults, every other
 parameter in turn is swept over its candidates with the rest fixed and the
 fastest value kept, two passes over all of them; the fastest of the per-
 pagesize results wins. Every candidate is measured
-on a fresh heap as the median of `repeats` CUDA-event-timed runs of the batch
-(one graph launch each) after three warm-up runs, so geometries that degrade
-as the heap ages are measured aged. Candidates whose runs fail
-a job (a null allocation or a pattern error) are rejected.
+on a fresh heap: the slower of two medians of `repeats` CUDA-event-timed runs
+of the batch (one graph launch each), after three warm-up runs and after forty
+more, so geometries that degrade as the heap ages are measured aged.
+Candidates whose runs fail a job (a null allocation or a pattern error) are
+rejected.
 """
 from __future__ import annotations
 
@@ -51,10 +52,13 @@ def _accessblock(heap_bytes: int, pagesize: int, fraction: int) -> int:
 
 
 def measure(cfg: TuneConfig, jobs, heap_bytes: int, device: int, sms: int, expected=None, repeats: int = 3,
-            warmups: int = 3):
-    """Median milliseconds of one batched (graph) run under cfg once the heap has
-    aged (after `warmups` runs: some geometries degrade as pages keep their
-    chunk formats and region counters fill), or None if a job failed."""
+            warmups: int = 3, aging: int = 40):
+    """Milliseconds of one batched (graph) run under cfg, or None if a job
+    failed: the larger of the median of `repeats` runs after `warmups` runs and
+    the median of `repeats` runs after `aging` more. Some geometries degrade as
+    the heap ages (pages keep their chunk formats, so a heap of many coalesced
+    sizes runs out of pages of the right size), a few of them only after tens
+    of runs."""
     import torch
 
     from .allocator import Allocator
@@ -75,20 +79,28 @@ def measure(cfg: TuneConfig, jobs, heap_bytes: int, device: int, sms: int, expec
             batch.run()
         torch.cuda.synchronize()
         batch.stats(clear=True)
-        times = []
-        for _ in range(repeats):
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
+
+        def timed():
+            times = []
+            for _ in range(repeats):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                batch.run()
+                e1.record(stream)
+                torch.cuda.synchronize()
+                times.append(e0.elapsed_time(e1))
+            return statistics.median(times)
+
+        early = timed()
+        for _ in range(aging):
             batch.run()
-            e1.record(stream)
-            torch.cuda.synchronize()
-            times.append(e0.elapsed_time(e1))
+        late = timed()
         st = batch.stats(clear=True)
         if int(st[:, 1].sum()) or int(st[:, 2].sum()):
             return None
-        if expected is not None and not np.array_equal(st[:, 0].astype(np.int64), repeats * expected):
+        if expected is not None and not np.array_equal(st[:, 0].astype(np.int64), (2 * repeats + aging) * expected):
             return None
-        return statistics.median(times)
+        return max(early, late)
     finally:
         if batch is not None:
             batch.close()

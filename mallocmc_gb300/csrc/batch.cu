@@ -63,11 +63,16 @@ namespace
 
     /* Size of cycle c of job thread jt: geometric on {1, 2, ...} with the job's
      * mean (inverse-CDF draw), capped, padded to 16. */
-    __device__ __forceinline__ uint32_t draw_size(const mmc_job& j, uint64_t m)
+    __device__ __forceinline__ float log_q(const mmc_job& j)
+    {
+        return logf(1.0f - 1.0f / static_cast<float>(j.mean_size));
+    }
+
+    /* logq = log_q(j), which a caller running many cycles of one job computes once */
+    __device__ __forceinline__ uint32_t draw_size(const mmc_job& j, uint64_t m, float logq)
     {
         const float u = (static_cast<float>(m >> 40) + 0.5f) * (1.0f / 16777216.0f); /* (0, 1) */
-        const float q = 1.0f - 1.0f / static_cast<float>(j.mean_size);
-        float x = 1.0f + floorf(logf(u) / logf(q));
+        float x = 1.0f + floorf(logf(u) / logq);
         if(!(x < static_cast<float>(j.max_size)))
             x = static_cast<float>(j.max_size);
         const uint32_t s = static_cast<uint32_t>(x);
@@ -80,10 +85,11 @@ namespace
     {
         const uint32_t span = j.max_cycles - j.min_cycles + 1u;
         const uint32_t cycles = j.min_cycles + static_cast<uint32_t>(mix64(j.seed, jt, 0xC1C1Eull) >> 32) % span;
+        const float logq = log_q(j);
         for(uint32_t c = 0; c < cycles; ++c)
         {
             const uint64_t m = mix64(j.seed, jt, c);
-            const uint32_t bytes = draw_size(j, m);
+            const uint32_t bytes = draw_size(j, m, logq);
             char* ptr = static_cast<char*>(dv::malloc<dv::GpuIds>(h, bytes));
             if(ptr == nullptr)
             {
@@ -175,6 +181,7 @@ __global__ void __launch_bounds__(256) mmc_batch_kernel(mmc_device_handle h, con
     const uint32_t lanes_below = (1u << lane) - 1u;
     uint32_t job = 0, jt = 0, cycles = 0, c = 0;
     uint64_t seed = 0;
+    float logq = 0.0f;
     mmc_job j{};
     bool done = false;
     unsigned long long pairs = 0, nulls = 0, bad = 0, csum = 0;
@@ -237,6 +244,7 @@ __global__ void __launch_bounds__(256) mmc_batch_kernel(mmc_device_handle h, con
                         const uint32_t span = j.max_cycles - j.min_cycles + 1u;
                         cycles = j.min_cycles + static_cast<uint32_t>(mix64(j.seed, jt, 0xC1C1Eull) >> 32) % span;
                         seed = j.seed;
+                        logq = log_q(j);
                         need = cycles == 0u; /* a thread with no cycles is done at once */
                     }
                 }
@@ -248,7 +256,7 @@ __global__ void __launch_bounds__(256) mmc_batch_kernel(mmc_device_handle h, con
         if(!done)
         {
             const uint64_t m = mix64(seed, jt, c);
-            const uint32_t bytes = draw_size(j, m);
+            const uint32_t bytes = draw_size(j, m, logq);
             char* ptr = static_cast<char*>(dv::malloc<dv::GpuIds>(h, bytes));
             if(ptr == nullptr)
                 ++nulls;
