@@ -163,6 +163,9 @@ STRESS_DRAM_BYTES_PER_PAIR = 587.0
 # formatted page's chunk size is loaded instead of CAS'd and same-size lanes
 # share one reservation.
 STRESS_NCU_ATOMICS_PER_PAIR = 4.01
+# L2 atomic requests per pair of the batched workload's persistent kernel, from
+# an ncu capture on the tuned geometry (profiles/mmc_batch_kernel_512jobs_8GiB.md).
+BATCH_NCU_ATOMICS_PER_PAIR = 0.208
 STRESS_TRAFFIC_NOTE = ("dram__bytes_read.sum + dram__bytes_write.sum per pair from an ncu capture of the same "
                        "kernel on a 2 GiB heap / 20 rounds, times the pairs of one launch")
 
@@ -302,32 +305,20 @@ def oldmalloc_column(torch, stream, heap_bytes, blocks, tpb, rounds, d_sizes, fl
             "rounds": rounds, "ms_per_launch": statistics.median(ms), "nulls": int(st[1]), "pattern_errors": int(st[2])}
 
 
-# The batched workload's geometry as chosen by mallocmc_gb300.autotune (a coordinate
-# descent over regionsize, hash primes, access block and grid per pagesize) on a
-# GB300 (`bench.py --autotune` re-runs it). Its two best points, 16 KiB pages with
-# the (38183, 17497) or the (7919, 101) hash primes, time within 0.3 % of each
-# other (2.33-2.34 ms per graph launch, flat over 60 launches on the 16 GiB heap);
-# on an 8 GiB heap the first collapses after about 45 launches (pages of the
-# right chunk size run out) while the second stays near 2.5 ms, so this is the
-# second.
-BATCH_TUNED = {"pagesize": 16384, "regionsize": 32, "hashingK": 7919, "hashingDistMP": 101,
-               "accessblock_fraction": 1, "blocks_per_sm": 8}
-
-
 def batched_column(torch, args, sms, atom_peak=None):
     """512 uneven jobs on one 16 GiB heap: one persistent graph-captured launch
     against one plain launch per job (same allocations, checked job by job).
     With atom_peak (measured L2 atomics/s), each form's algorithmic atomics per
     second (batched_algorithmic_atomics) against it."""
     from mallocmc_gb300 import AlignmentPolicies, Allocator, CreationPolicies, DistributionPolicies
-    from mallocmc_gb300.autotune import TuneConfig, _accessblock, autotune
+    from mallocmc_gb300.autotune import GB300_TUNED, TuneConfig, _accessblock, autotune
     from mallocmc_gb300.batch import Batch, expected_pairs, make_jobs
 
     heap_bytes = 16 << 30
     jobs = make_jobs(512, seed=3)
     want = expected_pairs(jobs)
     tune_trace = None
-    cfg = TuneConfig(**BATCH_TUNED)
+    cfg = GB300_TUNED
     if args.autotune:
         cfg, _, tune_trace = autotune(jobs, heap_bytes, expected=want)
 
@@ -374,8 +365,12 @@ def batched_column(torch, args, sms, atom_peak=None):
             return None
         w = batched_algorithmic_atomics(jobs, c.pagesize)
         ach = w["atomics"] / (ms * 1e-3)
-        return {"bound": "l2_atomic", "achieved": ach / 1e9, "peak": atom_peak / 1e9, "unit": "Gatomic/s",
-                "frac": ach / atom_peak, "atomics_per_pair": w["atomics_per_pair"], "form": "graph"}
+        out = {"bound": "l2_atomic", "achieved": ach / 1e9, "peak": atom_peak / 1e9, "unit": "Gatomic/s",
+               "frac": ach / atom_peak, "atomics_per_pair": w["atomics_per_pair"], "form": "graph"}
+        if c == GB300_TUNED:
+            out["ncu_atomics_per_pair"] = BATCH_NCU_ATOMICS_PER_PAIR
+            out["ncu_frac"] = pairs / (ms * 1e-3) * BATCH_NCU_ATOMICS_PER_PAIR / atom_peak
+        return out
 
     res = {"workload": "512 jobs on a 16 GiB heap, threads log-uniform in [32, 65536], sizes geometric "
                        "(mean 64 B, cap 4 KiB, padded to 16), 1-16 cycles per thread",

@@ -40,6 +40,17 @@ class TuneConfig:
     blocks_per_sm: int = 8
 
 
+# The geometry this search picks for the bench's batched workload (512 jobs,
+# make_jobs(512, seed=3), on a 16 GiB heap) on a GB300. Its two best points,
+# 16 KiB pages with the (38183, 17497) or the (7919, 101) hash primes, time
+# within 0.3 % of each other (2.33-2.34 ms per graph launch, flat over 60
+# launches on the 16 GiB heap); on an 8 GiB heap the first collapses after
+# about 45 launches (pages of the right chunk size run out) while the second
+# stays near 2.5 ms, so this is the second.
+GB300_TUNED = TuneConfig(pagesize=16384, regionsize=32, hashingK=7919, hashingDistMP=101, accessblock_fraction=1,
+                         blocks_per_sm=8)
+
+
 def _accessblock(heap_bytes: int, pagesize: int, fraction: int) -> int:
     """An access block that divides the page area into `fraction` blocks (the
     page area is slightly smaller than the heap: metadata takes its share);

@@ -75,3 +75,64 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+
+def main(argv=None):
+    """Run the uneven-job workload (make_jobs) on a fresh heap of the given size
+    and geometry (default: autotune.GB300_TUNED), check every job's pair count,
+    nulls and pattern errors, and print the milliseconds of each run.
+    `--no-graph` launches the persistent kernel directly instead of replaying
+    its graph (so a profiler sees a plain launch), `--plain` one launch per job."""
+    import argparse
+    import json
+    import time
+
+    import torch
+
+    from .autotune import GB300_TUNED, _accessblock
+    from .policies import AlignmentPolicies, CreationPolicies, DistributionPolicies
+
+    ap = argparse.ArgumentParser(prog="python -m mallocmc_gb300.batch")
+    ap.add_argument("--jobs", type=int, default=512)
+    ap.add_argument("--seed", type=int, default=3)
+    ap.add_argument("--heap-gib", type=int, default=16)
+    ap.add_argument("--runs", type=int, default=2)
+    ap.add_argument("--pagesize", type=int, default=GB300_TUNED.pagesize)
+    ap.add_argument("--regionsize", type=int, default=GB300_TUNED.regionsize)
+    ap.add_argument("--hashingK", type=int, default=GB300_TUNED.hashingK)
+    ap.add_argument("--hashingDistMP", type=int, default=GB300_TUNED.hashingDistMP)
+    ap.add_argument("--accessblock-fraction", type=int, default=GB300_TUNED.accessblock_fraction)
+    ap.add_argument("--blocks-per-sm", type=int, default=GB300_TUNED.blocks_per_sm)
+    form = ap.add_mutually_exclusive_group()
+    form.add_argument("--no-graph", action="store_true")
+    form.add_argument("--plain", action="store_true")
+    a = ap.parse_args(argv)
+
+    heap_bytes = a.heap_gib << 30
+    jobs = make_jobs(a.jobs, seed=a.seed)
+    want = expected_pairs(jobs)
+    creation = CreationPolicies.Scatter(pagesize=a.pagesize, regionsize=a.regionsize,
+                                        accessblocksize=_accessblock(heap_bytes, a.pagesize, a.accessblock_fraction),
+                                        hashingK=a.hashingK, hashingDistMP=a.hashingDistMP)
+    alloc = Allocator(creation, DistributionPolicies.XMallocSIMD(a.pagesize), None, None,
+                      AlignmentPolicies.Shrink(16), size=heap_bytes)
+    sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    b = Batch(alloc, jobs, persistent_blocks=sms * a.blocks_per_sm, use_graph=not a.no_graph)
+    ms = []
+    for _ in range(a.runs):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        b.run_plain() if a.plain else b.run()
+        torch.cuda.synchronize()
+        ms.append(1e3 * (time.perf_counter() - t0))
+    st = b.stats(clear=True)
+    ok = (np.array_equal(st[:, 0].astype(np.int64), a.runs * want) and int(st[:, 1].sum()) == 0
+          and int(st[:, 2].sum()) == 0)
+    b.close()
+    alloc.close()
+    print(json.dumps({"ok": ok, "pairs_per_run": int(want.sum()), "ms_per_run_host": ms}))
+    return 0 if ok else 1
+
+
+if __name__ == "__main__":
+    raise SystemExit(main())
