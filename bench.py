@@ -157,12 +157,12 @@ def batched_algorithmic_atomics(jobs, pagesize: int) -> dict:
 # ncu capture (dram__bytes_read.sum + dram__bytes_write.sum) of the same kernel on
 # a 2 GiB heap with 20 rounds (profiles/mmc_stress_kernel_uniform_2GiB_20rounds.md);
 # almost all of it is the write-back of the written payload, so it scales with pairs.
-STRESS_DRAM_BYTES_PER_PAIR = 587.0
+STRESS_DRAM_BYTES_PER_PAIR = 586.0
 # L2 atomic requests per pair counted by ncu (lts__t_requests_srcunit_tex_op_atom*
 # + op_red) in the same capture: below the reference algorithm's 4.72 because a
 # formatted page's chunk size is loaded instead of CAS'd and same-size lanes
 # share one reservation.
-STRESS_NCU_ATOMICS_PER_PAIR = 4.01
+STRESS_NCU_ATOMICS_PER_PAIR = 3.93
 # L2 atomic requests per pair of the batched workload's persistent kernel, from
 # an ncu capture on the tuned geometry (profiles/mmc_batch_kernel_512jobs_8GiB.md).
 BATCH_NCU_ATOMICS_PER_PAIR = 0.208
