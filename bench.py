@@ -155,9 +155,10 @@ def batched_algorithmic_atomics(jobs, pagesize: int) -> dict:
 
 # DRAM bytes (read + written) per malloc+free pair of the stress kernel, from one
 # ncu capture (dram__bytes_read.sum + dram__bytes_write.sum) of the same kernel on
-# a 2 GiB heap with 20 rounds (profiles/mmc_stress_kernel_uniform_2GiB_20rounds.md);
-# almost all of it is the write-back of the written payload, so it scales with pairs.
-STRESS_DRAM_BYTES_PER_PAIR = 586.0
+# a 2 GiB heap with 20 rounds (profiles/mmc_stress_kernel_uniform_2GiB_20rounds.md):
+# the partial lines at the blocks' ends (their whole lines are discarded from L2
+# before the free) and the metadata, so it scales with pairs.
+STRESS_DRAM_BYTES_PER_PAIR = 172.0
 # L2 atomic requests per pair counted by ncu (lts__t_requests_srcunit_tex_op_atom*
 # + op_red) in the same capture: below the reference algorithm's 4.72 because a
 # formatted page's chunk size is loaded instead of CAS'd and same-size lanes

@@ -1160,6 +1160,38 @@ namespace mmc
             destroy<Ids>(h, p);
         }
 
+        /* For a caller about to free a block whose contents are dead: drop the
+         * whole 128-byte lines inside [p, p + bytes) from L2 without writing
+         * them back to DRAM (discard.global.L2; their bytes become
+         * indeterminate), then read one word of each line through L2. The
+         * returned pointer equals p but depends on those reads, so a free of
+         * it is issued only after every discard has taken effect in L2 and no
+         * later owner's writes can be discarded. Partial lines at the ends are
+         * left alone (they may hold a neighbouring block). No counterpart in
+         * the reference: a short-lived block's payload otherwise costs a DRAM
+         * write-back after it is freed. */
+        __device__ __forceinline__ void* discard_dead_block(void* p, u32 bytes)
+        {
+            const u64 a = reinterpret_cast<u64>(p);
+            const u64 lo = (a + 127ull) & ~127ull;
+            const u64 end = a + bytes;
+            for(u64 x = lo; x + 128ull <= end; x += 128ull)
+                asm volatile("discard.global.L2 [%0], 128;" ::"l"(x) : "memory");
+            u32 token = 0u;
+            for(u64 x = lo; x + 128ull <= end; x += 128ull)
+            {
+                u32 v;
+                asm volatile("ld.global.cg.u32 %0, [%1];" : "=r"(v) : "l"(x) : "memory");
+                token |= v;
+            }
+            void* r;
+            asm volatile("{\n\t.reg .u32 z;\n\t.reg .u64 z64;\n\tand.b32 z, %2, 0;\n\tcvt.u64.u32 z64, z;\n\t"
+                         "add.u64 %0, %1, z64;\n\t}"
+                         : "=l"(r)
+                         : "l"(p), "r"(token));
+            return r;
+        }
+
         /* ------------------------------------------------ free-slot counting */
 
         /* Run summary of a page range for the multi-page slot count: the
