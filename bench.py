@@ -18,7 +18,9 @@ uniform in {16, 32, ..., 1024}, drawn from a seeded SplitMix64 table
                    with its own atomic roofline (the reference algorithm's atomics for
                    the jobs' draws against the same measured peak)
   serving          the continuous-batching request loop: p50/p99 latency and throughput
-  fragmentation    fill at out-of-memory against the oracle's serial run
+                   (and each row's atomic fraction)
+  fragmentation    fill at out-of-memory against the oracle's serial run (and the run's
+                   atomic fraction)
   cpu_baseline     the oracle port of the reference's CPU backend on the host cores
 
 `--impl reference` times the reference's CPU implementation of the path (the
@@ -388,7 +390,7 @@ def batched_column(torch, args, sms, atom_peak=None):
     return res
 
 
-def serving_column(torch, args):
+def serving_column(torch, args, atom_peak=None):
     """Continuous batching on a 64 GiB device-resident heap (pagesize 64 KiB, so a
     16 KiB chunk is a plain chunk): Poisson arrivals at each rate, lognormal
     lengths (median 1024, sigma 1, cap 32768 elements of 2 B), one 16 KiB chunk per
@@ -422,6 +424,9 @@ def serving_column(torch, args):
                          "throughput_req_per_s": ok.sum() / span if ok.any() else 0.0,
                          "chunks_per_s": float((-(-lengths[ok] // 256)).sum() / span) if ok.any() else 0.0,
                          "ticks": res["ticks"]})
+            if atom_peak:
+                # a 16 KiB chunk on a 64 KiB page: malloc 3 atomics, free 2 (reference algorithm)
+                rows[-1]["atomic_frac"] = rows[-1]["chunks_per_s"] * 5 / atom_peak
     srv.close()
     alloc.close()
     return {"workload": "64 GiB heap, pagesize 64 KiB; Poisson arrivals; lognormal lengths (median 1024, sigma 1, "
@@ -432,7 +437,7 @@ def serving_column(torch, args):
 FRAG_GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tests", "golden", "frag_fill.json")
 
 
-def fragmentation_column(torch, args, sms):
+def fragmentation_column(torch, args, sms, atom_peak=None):
     """Fill until the first NULL, free a seeded half, refill until the next NULL
     on a 32 GiB heap (pagesize 4096, 256 MiB access blocks): 90 % of requests
     uniform in [16, 2048] B, 10 % log-uniform in [8 KiB, 1 MiB]. Requests go out
@@ -464,6 +469,12 @@ def fragmentation_column(torch, args, sms):
         r["error_flags"] = alloc.error_flags()
         alloc.close()
         r["hash"] = {"hashingDistMP": mp, "hashingDistWP": wp, "hashingDistWPRel": wprel}
+        if atom_peak:
+            r["atomic_roofline"] = {"bound": "l2_atomic", "achieved": r["atomics_per_second"] / 1e9,
+                                    "peak": atom_peak / 1e9, "unit": "Gatomic/s",
+                                    "frac": r["atomics_per_second"] / atom_peak,
+                                    "note": "reference algorithm's minimum atomics of the run's mallocs and frees "
+                                            "(fragmentation.run_fragmentation) / run time"}
         if ref is not None:
             r["fill_vs_reference"] = {"phase1": r["phase1_fill"] - ref["phase1_fill"],
                                       "final": r["final_fill"] - ref["final_fill"]}
@@ -718,10 +729,10 @@ def main():
         batched = batched_column(torch, args, sms, pk["atom_l2_32MiB"] if pk else None)
     serving = None
     if not args.no_serve:
-        serving = serving_column(torch, args)
+        serving = serving_column(torch, args, pk["atom_l2_32MiB"] if pk else None)
     frag = None
     if not args.no_frag:
-        frag = fragmentation_column(torch, args, sms)
+        frag = fragmentation_column(torch, args, sms, pk["atom_l2_32MiB"] if pk else None)
     oldm = None
     if not args.no_oldmalloc:
         oldm = oldmalloc_column(torch, stream, heap_bytes, blocks, tpb, args.oldmalloc_rounds, d_sizes, flush, pattern)

@@ -81,7 +81,19 @@ def run_fragmentation(alloc: Allocator, seed: int, blocks: int, threads_per_bloc
     torch.cuda.synchronize(dev)
     c = ctr.cpu().numpy().view(np.uint64)
     ops = req_total + len(half)
+    # minimum global atomics of these operations under the reference algorithm:
+    # chunked malloc 3 (CAS chunk size, add count, or mask), k-page malloc k CASes
+    # + the hint CAS; chunked free 2 (3 on a hierarchical chunk), k-page free k
+    # CASes + the hint max; a failing malloc none
+    pagesize = int(alloc.getAllocatorHandle().pagesize)
+    got = sizes[: min(n_total, capacity)].cpu().numpy().astype(np.int64)
+    pages = -(-got // pagesize)
+    atomics = int(np.where(got <= pagesize, 3, pages + 1).sum())
+    fs = got[half[half < len(got)]]
+    ht = (pagesize - 8) // 33
+    atomics += int(np.where(fs <= pagesize, np.where(fs <= ht, 3, 2), -(-fs // pagesize) + 1).sum())
     out.update(freed=len(half), phase2_allocs=n_total - n1, final_live_bytes=live2, final_fill=live2 / heap_bytes,
+               algorithmic_atomics=atomics, atomics_per_second=atomics / (t1 + tf + t2),
                tag_errors=int(c[3]), free_seconds=tf, phase2_seconds=t2,
                ops_per_second=ops / (t1 + tf + t2), list_overflow=n_total > capacity, wave_requests=T,
                waves=(w1, w2))
