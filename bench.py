@@ -409,9 +409,9 @@ def serving_column(torch, args, atom_peak=None):
         n = int(min(rate * args.serve_seconds, 50000))
         arrivals, lengths, seeds = make_requests(n, rate, seed=rate)
         want = np.array([expected_checksum(int(s), int(l)) for s, l in zip(seeds, lengths)], dtype=np.uint64)
-        for mode in ("graph_per_tick", "launch_per_request"):
-            res = srv.run(arrivals, lengths, seeds, batched=(mode == "graph_per_tick"), realtime=True,
-                          max_seconds=max(5.0, 4 * args.serve_seconds))
+        for mode in ("graph_pipelined", "graph_per_tick", "launch_per_request"):
+            res = srv.run(arrivals, lengths, seeds, batched=(mode != "launch_per_request"), realtime=True,
+                          max_seconds=max(5.0, 4 * args.serve_seconds), pipelined=(mode == "graph_pipelined"))
             ok = ~np.isnan(res["done"])
             lat = (res["done"] - res["admit"])[ok] * 1e3
             qlat = (res["done"] - arrivals)[ok] * 1e3

@@ -415,6 +415,28 @@ mmc_status mmc_serve_queue(mmc_server* server, mmc_serve_cmd** queue, uint32_t**
 /* Run one tick and wait for it: batched != 0 replays the captured graph (all
  * live requests in one launch); 0 launches one kernel per live request. */
 mmc_status mmc_serve_tick(mmc_server* server, int batched);
+
+/* Pipelined ticks: two buffers (b = 0, 1), each with its own command queue and
+ * its own results, so the host reads one tick's results and writes the next
+ * tick's commands while a tick runs. A tick launched on buffer b applies queue
+ * b, grows every live request, and publishes into buffer b: the requests that
+ * completed in it (slot and checksum), the chunks the still-live requests will
+ * yet take (sum of ceil(final_len / 256) - nchunks) and the free 16 KiB chunk
+ * count at its end. */
+typedef struct mmc_serve_done
+{
+    uint32_t slot;
+    uint32_t reserved;
+    uint64_t checksum;
+} mmc_serve_done;
+
+mmc_status mmc_serve_pipeline(mmc_server* server, int buffer, mmc_serve_cmd** queue, uint32_t** queue_len,
+                              mmc_serve_done** done, uint32_t** done_len, unsigned long long** remaining,
+                              unsigned** free_chunks);
+/* Launch the batched tick on `buffer` without waiting for it. */
+mmc_status mmc_serve_launch(mmc_server* server, int buffer);
+/* Wait for every tick launched so far. */
+mmc_status mmc_serve_wait(mmc_server* server);
 mmc_status mmc_serve_destroy(mmc_server* server);
 
 /* Relaxed device-scope atomicOr throughput over `words` u32 words at `buf`

@@ -18,6 +18,13 @@
  * the host's copy of the slot table, and the free-chunk count lands in host
  * memory, so a tick has no copy steps (on GB300 the device reaches host
  * memory over NVLink-C2C).
+ *
+ * Pipelined ticks alternate between two buffers, each with its own command
+ * queue and its own published results (the requests that completed in the
+ * tick, with their checksums; the chunks the live requests will yet take; the
+ * free-chunk count). While tick i runs on one buffer, the host reads what tick
+ * i - 1 published in the other and writes tick i + 1's commands there, so host
+ * and device work overlap and the host never reads what a running tick writes.
  */
 #include "mmc_internal.h"
 
@@ -65,6 +72,29 @@ struct mmc_server
     cudaStream_t stream;
     cudaGraphExec_t exec;
     cudaGraph_t graph;
+    /* pipelined ticks: per buffer a command queue and the tick's published
+     * results (mapped pinned, h_* the host's addresses and m_* the device's),
+     * the completion list and counters the tick builds in device memory, and
+     * the captured tick graph */
+    struct Pipe
+    {
+        mmc_serve_cmd* h_queue;
+        uint32_t* h_queue_len;
+        const mmc_serve_cmd* m_queue;
+        const uint32_t* m_queue_len;
+        mmc_serve_done* h_done;
+        uint32_t* h_done_len;
+        unsigned long long* h_remaining;
+        unsigned* h_free;
+        mmc_serve_done* m_done;
+        uint32_t* m_done_len;
+        unsigned long long* m_remaining;
+        unsigned* m_free;
+        mmc_serve_done* d_done;
+        unsigned long long* d_counts; /* [0]: completions, [1]: chunks still to take */
+        cudaGraph_t graph;
+        cudaGraphExec_t exec;
+    } pipe[2];
 };
 
 /* Apply admissions (cmd.kind 1) and releases (cmd.kind 2), read from the
@@ -162,10 +192,14 @@ __device__ __forceinline__ void grow_request(const mmc_device_handle& h, mmc_ser
     }
 }
 
-/* Batched tick: one warp per slot; each grown slot is written to the host's table. */
+/* Batched tick: one warp per slot; each grown slot is written to the host's
+ * table. With `done` (pipelined ticks), a request that completes here is also
+ * appended to the completion list, and each request still live adds the chunks
+ * it will yet take to counts[1] (counts[0] is the list's length). */
 __global__ void __launch_bounds__(256) mmc_serve_tick_kernel(mmc_device_handle h, mmc_serve_slot* slots,
                                                              mmc_serve_slot* mirror, void** chunks, uint32_t nslots,
-                                                             uint32_t max_chunks, uint32_t step)
+                                                             uint32_t max_chunks, uint32_t step,
+                                                             mmc_serve_done* done, unsigned long long* counts)
 {
     const uint32_t warps = gridDim.x * (blockDim.x / 32u);
     for(uint32_t w = blockIdx.x * (blockDim.x / 32u) + threadIdx.x / 32u; w < nslots; w += warps)
@@ -175,7 +209,41 @@ __global__ void __launch_bounds__(256) mmc_serve_tick_kernel(mmc_device_handle h
         grow_request(h, slots[w], chunks + static_cast<uint64_t>(w) * max_chunks, max_chunks, step);
         __syncwarp();
         if((threadIdx.x & 31u) == 0u)
-            mirror[w] = slots[w];
+        {
+            const mmc_serve_slot sw = slots[w];
+            mirror[w] = sw;
+            if(done != nullptr)
+            {
+                if(sw.state == MMC_SERVE_DONE)
+                {
+                    const unsigned long long i = atomicAdd(&counts[0], 1ull);
+                    done[i] = mmc_serve_done{w, 0u, sw.checksum};
+                }
+                else
+                {
+                    const uint32_t need = (sw.final_len + kElemsPerChunk - 1u) / kElemsPerChunk;
+                    atomicAdd(&counts[1], static_cast<unsigned long long>(need - sw.nchunks));
+                }
+            }
+        }
+    }
+}
+
+/* End of a pipelined tick: publish its completion list and counters to the
+ * host (mapped memory) and zero the counters for the tick after next. One block. */
+__global__ void mmc_serve_publish(const mmc_serve_done* done, unsigned long long* counts, mmc_serve_done* out,
+                                  uint32_t* out_len, unsigned long long* out_remaining)
+{
+    const uint32_t n = static_cast<uint32_t>(counts[0]);
+    for(uint32_t i = threadIdx.x; i < n; i += blockDim.x)
+        out[i] = done[i];
+    __syncthreads();
+    if(threadIdx.x == 0)
+    {
+        *out_len = n;
+        *out_remaining = counts[1];
+        counts[0] = 0ull;
+        counts[1] = 0ull;
     }
 }
 
@@ -209,6 +277,21 @@ namespace
         cudaFreeHost(s->h_queue_len);
         cudaFreeHost(s->h_slots);
         cudaFreeHost(s->h_free);
+        for(auto& p : s->pipe)
+        {
+            if(p.exec)
+                cudaGraphExecDestroy(p.exec);
+            if(p.graph)
+                cudaGraphDestroy(p.graph);
+            cudaFreeHost(p.h_queue);
+            cudaFreeHost(p.h_queue_len);
+            cudaFreeHost(p.h_done);
+            cudaFreeHost(p.h_done_len);
+            cudaFreeHost(p.h_remaining);
+            cudaFreeHost(p.h_free);
+            cudaFree(p.d_done);
+            cudaFree(p.d_counts);
+        }
         delete s;
     }
 
@@ -222,12 +305,40 @@ namespace
         {
             const uint32_t blocks = (s->slots + 7u) / 8u;
             mmc_serve_tick_kernel<<<blocks, 256, 0, st>>>(s->handle, s->d_slots, s->m_slots, s->d_chunks, s->slots,
-                                                         s->max_chunks, s->step);
+                                                         s->max_chunks, s->step, nullptr, nullptr);
         }
         mmc_status r = mmc_available_slots_async(s->heap, kChunkBytes, st, s->m_free);
         if(r != MMC_OK)
             return r;
         return cuda_check(cudaGetLastError(), "serve tick");
+    }
+    /* A pipelined tick on buffer b: apply its queue, grow, count the free
+     * chunks into its mapped count, publish its completions. */
+    mmc_status enqueue_pipelined_tick(mmc_server* s, int b)
+    {
+        cudaStream_t st = s->stream;
+        mmc_server::Pipe& p = s->pipe[b];
+        mmc_serve_apply<<<8, 128, 0, st>>>(s->d_slots, s->m_slots, p.m_queue, p.m_queue_len);
+        const uint32_t blocks = (s->slots + 7u) / 8u;
+        mmc_serve_tick_kernel<<<blocks, 256, 0, st>>>(s->handle, s->d_slots, s->m_slots, s->d_chunks, s->slots,
+                                                     s->max_chunks, s->step, p.d_done, p.d_counts);
+        mmc_status r = mmc_available_slots_async(s->heap, kChunkBytes, st, p.m_free);
+        if(r != MMC_OK)
+            return r;
+        mmc_serve_publish<<<1, 256, 0, st>>>(p.d_done, p.d_counts, p.m_done, p.m_done_len, p.m_remaining);
+        return cuda_check(cudaGetLastError(), "pipelined serve tick");
+    }
+
+    /* cudaHostAlloc(mapped) + its device address */
+    template<class T>
+    mmc_status mapped(T** host, T** dev, size_t bytes, const char* what)
+    {
+        mmc_status st = cuda_check(cudaHostAlloc(reinterpret_cast<void**>(host), bytes, cudaHostAllocMapped), what);
+        if(st == MMC_OK)
+            st = cuda_check(cudaHostGetDevicePointer(reinterpret_cast<void**>(dev), *host, 0), what);
+        if(st == MMC_OK)
+            std::memset(*host, 0, bytes);
+        return st;
     }
 } // namespace
 
@@ -302,6 +413,42 @@ mmc_status mmc_serve_create(mmc_heap* heap, uint32_t slots, uint32_t max_chunks,
     }
     if(st == MMC_OK)
         st = cuda_check(cudaGraphInstantiate(&s->exec, s->graph, 0), "instantiate tick graph");
+    for(int b = 0; b < 2 && st == MMC_OK; ++b)
+    {
+        mmc_server::Pipe& p = s->pipe[b];
+        mmc_serve_cmd* mq = nullptr;
+        uint32_t* mql = nullptr;
+        st = mapped(&p.h_queue, &mq, sizeof(mmc_serve_cmd) * queue_cap, "pipelined queue");
+        p.m_queue = mq;
+        if(st == MMC_OK)
+            st = mapped(&p.h_queue_len, &mql, sizeof(uint32_t), "pipelined queue length");
+        p.m_queue_len = mql;
+        if(st == MMC_OK)
+            st = mapped(&p.h_done, &p.m_done, sizeof(mmc_serve_done) * slots, "completion list");
+        if(st == MMC_OK)
+            st = mapped(&p.h_done_len, &p.m_done_len, sizeof(uint32_t), "completion count");
+        if(st == MMC_OK)
+            st = mapped(&p.h_remaining, &p.m_remaining, sizeof(unsigned long long), "chunks still to take");
+        if(st == MMC_OK)
+            st = mapped(&p.h_free, &p.m_free, sizeof(unsigned), "pipelined free count");
+        if(st == MMC_OK)
+            st = cuda_check(cudaMalloc(&p.d_done, sizeof(mmc_serve_done) * slots), "device completion list");
+        if(st == MMC_OK)
+            st = cuda_check(cudaMalloc(&p.d_counts, 2 * sizeof(unsigned long long)), "device completion counts");
+        if(st == MMC_OK)
+            st = cuda_check(cudaMemset(p.d_counts, 0, 2 * sizeof(unsigned long long)), "zero completion counts");
+        if(st == MMC_OK)
+            st = cuda_check(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
+        if(st == MMC_OK)
+        {
+            mmc_status e = enqueue_pipelined_tick(s, b);
+            st = cuda_check(cudaStreamEndCapture(s->stream, &p.graph), "end capture");
+            if(st == MMC_OK)
+                st = e;
+        }
+        if(st == MMC_OK)
+            st = cuda_check(cudaGraphInstantiate(&p.exec, p.graph, 0), "instantiate pipelined tick graph");
+    }
     if(st != MMC_OK)
     {
         release(s);
@@ -309,6 +456,42 @@ mmc_status mmc_serve_create(mmc_heap* heap, uint32_t slots, uint32_t max_chunks,
     }
     *out = s;
     return MMC_OK;
+}
+
+mmc_status mmc_serve_pipeline(mmc_server* s, int buffer, mmc_serve_cmd** queue, uint32_t** queue_len,
+                              mmc_serve_done** done, uint32_t** done_len, unsigned long long** remaining,
+                              unsigned** free_chunks)
+{
+    if(s == nullptr || buffer < 0 || buffer > 1)
+        return fail(MMC_ERR_ARG, "server is null or buffer not 0 or 1");
+    mmc_server::Pipe& p = s->pipe[buffer];
+    if(queue)
+        *queue = p.h_queue;
+    if(queue_len)
+        *queue_len = p.h_queue_len;
+    if(done)
+        *done = p.h_done;
+    if(done_len)
+        *done_len = p.h_done_len;
+    if(remaining)
+        *remaining = p.h_remaining;
+    if(free_chunks)
+        *free_chunks = p.h_free;
+    return MMC_OK;
+}
+
+mmc_status mmc_serve_launch(mmc_server* s, int buffer)
+{
+    if(s == nullptr || buffer < 0 || buffer > 1)
+        return fail(MMC_ERR_ARG, "server is null or buffer not 0 or 1");
+    return cuda_check(cudaGraphLaunch(s->pipe[buffer].exec, s->stream), "pipelined tick launch");
+}
+
+mmc_status mmc_serve_wait(mmc_server* s)
+{
+    if(s == nullptr)
+        return fail(MMC_ERR_ARG, "server is null");
+    return cuda_check(cudaStreamSynchronize(s->stream), "wait for ticks");
 }
 
 mmc_status mmc_serve_queue(mmc_server* s, mmc_serve_cmd** queue, uint32_t** queue_len, mmc_serve_slot** slots,

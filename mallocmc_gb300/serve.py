@@ -21,6 +21,7 @@ ELEMS_PER_CHUNK = 256
 SLOT_DTYPE = np.dtype([("id", "<u4"), ("final_len", "<u4"), ("len", "<u4"), ("nchunks", "<u4"), ("seed", "<u8"),
                        ("state", "<u4"), ("failed", "<u4"), ("checksum", "<u8")])
 CMD_DTYPE = np.dtype([("kind", "<u4"), ("slot", "<u4"), ("id", "<u4"), ("final_len", "<u4"), ("seed", "<u8")])
+DONE_DTYPE = np.dtype([("slot", "<u4"), ("reserved", "<u4"), ("checksum", "<u8")])
 
 
 def make_requests(n: int, rate: float, seed: int = 5, median: int = 1024, sigma: float = 1.0, cap: int = 32768):
@@ -65,9 +66,34 @@ class Server:
         # field views made once (a structured-array field lookup costs a microsecond a time)
         self._state, self._nchunks, self._checksum = (self.slots[f] for f in ("state", "nchunks", "checksum"))
         self._q = {f: self.queue[f] for f in ("kind", "slot", "id", "final_len", "seed")}
+        self._pipe = [self._pipe_views(b) for b in (0, 1)]
+
+    def _pipe_views(self, b):
+        """Host views of pipelined-tick buffer b: its command queue and the
+        results its tick publishes (completions, chunks still to take, free count)."""
+        ptrs = [ctypes.c_void_p() for _ in range(6)]
+        L.check(L.lib().mmc_serve_pipeline(self._s, b, *[ctypes.byref(x) for x in ptrs]), "serve_pipeline")
+
+        def arr(p, ctype, n):
+            return np.ctypeslib.as_array(ctypes.cast(p, ctypes.POINTER(ctype)), shape=(n,))
+
+        queue = arr(ptrs[0], ctypes.c_uint8, self.queue_cap * CMD_DTYPE.itemsize).view(CMD_DTYPE)
+        done = arr(ptrs[2], ctypes.c_uint8, self.nslots * DONE_DTYPE.itemsize).view(DONE_DTYPE)
+        return {"q": {f: queue[f] for f in ("kind", "slot", "id", "final_len", "seed")},
+                "qlen": arr(ptrs[1], ctypes.c_uint32, 1),
+                "done_slot": done["slot"], "done_checksum": done["checksum"],
+                "done_len": arr(ptrs[3], ctypes.c_uint32, 1),
+                "remaining": arr(ptrs[4], ctypes.c_uint64, 1),
+                "free": arr(ptrs[5], ctypes.c_uint32, 1)}
 
     def tick(self, batched: bool = True):
         L.check(L.lib().mmc_serve_tick(self._s, int(batched)), "serve_tick")
+
+    def launch(self, buffer: int):
+        L.check(L.lib().mmc_serve_launch(self._s, buffer), "serve_launch")
+
+    def wait(self):
+        L.check(L.lib().mmc_serve_wait(self._s), "serve_wait")
 
     def close(self):
         if getattr(self, "_s", None):
@@ -80,7 +106,103 @@ class Server:
         except Exception:
             pass
 
-    def run(self, arrivals, lengths, seeds, batched: bool = True, realtime: bool = True, max_seconds: float = 60.0):
+    def run_pipelined(self, arrivals, lengths, seeds, realtime: bool = True, max_seconds: float = 60.0):
+        """run() with batched ticks in flight while the host works: tick i runs on
+        buffer i % 2 with the queue the host built during tick i - 1, from the
+        results tick i - 2 published in the same buffer. The host therefore
+        never reads what a running tick writes, and a tick's period is the
+        longer of the device's and the host's work instead of their sum.
+        Admission counts against the free chunks of tick i - 2, less the chunks
+        its live requests will yet take and the needs admitted in the queue of
+        the tick in flight (completions of the tick in flight are not yet
+        counted, so admission stays on the safe side)."""
+        n = len(arrivals)
+        arrivals = np.asarray(arrivals)
+        lengths = np.asarray(lengths, dtype=np.int64)
+        seeds = np.asarray(seeds, dtype=np.int64)
+        need = -(-lengths // ELEMS_PER_CHUNK)
+        admit_t = np.full(n, np.nan)
+        done_t = np.full(n, np.nan)
+        checksum = np.zeros(n, dtype=np.uint64)
+        w_lo = 0
+        free_slots = list(range(self.nslots - 1, -1, -1))
+        slot_req = np.full(self.nslots, -1, dtype=np.int64)
+        if self.queue_cap < self.nslots:
+            raise ValueError("pipelined ticks need queue_cap >= slots (a tick may release every slot)")
+        ticks = 0
+        done = 0
+        P = self._pipe
+        # two empty ticks publish the starting free count into both buffers
+        for b in (0, 1):
+            P[b]["qlen"][0] = 0
+            self.launch(b)
+        self.wait()
+        inflight_pending = 0
+        released_inflight = []
+        i = 0
+        t0 = time.perf_counter()
+        while done < n:
+            now = time.perf_counter() - t0
+            if now > max_seconds:
+                break
+            nxt = n if not realtime else int(np.searchsorted(arrivals, now, side="right"))
+            pb = P[i & 1]
+            q = pb["q"]
+            # completions published by tick i - 2 in this buffer: released by this tick's queue
+            nd = int(pb["done_len"][0])
+            cmds = 0
+            released = []
+            if nd:
+                sl = pb["done_slot"][:nd].astype(np.int64)
+                r = slot_req[sl]
+                done_t[r] = now
+                checksum[r] = pb["done_checksum"][:nd]
+                done += nd
+                slot_req[sl] = -1
+                q["kind"][:nd] = 2
+                q["slot"][:nd] = sl
+                q["id"][:nd] = 0
+                q["final_len"][:nd] = 0
+                q["seed"][:nd] = 0
+                cmds = nd
+                released = sl.tolist()
+            free_slots.extend(released_inflight)  # released by the queue of the tick in flight
+            available = int(pb["free"][0]) - int(pb["remaining"][0]) - inflight_pending
+            pending = 0
+            k = min(nxt - w_lo, len(free_slots), self.queue_cap - cmds)
+            if k > 0:
+                k = int(np.searchsorted(np.cumsum(need[w_lo:w_lo + k]), available, side="right"))
+            if k > 0:
+                reqs = np.arange(w_lo, w_lo + k)
+                taken = np.asarray(free_slots[len(free_slots) - k:][::-1], dtype=np.int64)
+                del free_slots[len(free_slots) - k:]
+                slot_req[taken] = reqs
+                sl = slice(cmds, cmds + k)
+                q["kind"][sl] = 1
+                q["slot"][sl] = taken
+                q["id"][sl] = reqs
+                q["final_len"][sl] = lengths[reqs]
+                q["seed"][sl] = seeds[reqs].astype(np.uint64)
+                admit_t[reqs] = now
+                pending = int(need[reqs].sum())
+                cmds += k
+                w_lo += k
+            pb["qlen"][0] = cmds
+            self.wait()  # tick i - 1
+            self.launch(i & 1)
+            ticks += 1
+            i += 1
+            inflight_pending = pending
+            released_inflight = released
+        self.wait()
+        seconds = time.perf_counter() - t0
+        if done < n:
+            self._drain(slot_req)
+        return {"admit": admit_t, "done": done_t, "checksum": checksum, "ticks": ticks, "seconds": seconds,
+                "completed": done}
+
+    def run(self, arrivals, lengths, seeds, batched: bool = True, realtime: bool = True, max_seconds: float = 60.0,
+            pipelined: bool = False):
         """Serve the requests; returns a dict of per-request admit / done times
         (seconds from start), checksums, and loop counters. With realtime=False
         every request is treated as arrived at the start (used by tests).
@@ -89,7 +211,10 @@ class Server:
         longest prefix of the waiting requests whose expected chunks fit the
         free-chunk count (less the chunks live requests will still take) and
         for which a server slot is free. All per-tick work on the host is
-        vector operations over the slot table and the waiting range."""
+        vector operations over the slot table and the waiting range. With
+        pipelined (batched ticks only), run_pipelined serves instead."""
+        if pipelined and batched:
+            return self.run_pipelined(arrivals, lengths, seeds, realtime=realtime, max_seconds=max_seconds)
         n = len(arrivals)
         arrivals = np.asarray(arrivals)
         lengths = np.asarray(lengths, dtype=np.int64)

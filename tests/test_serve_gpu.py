@@ -31,6 +31,9 @@ def test_mix_and_alone_checksums_equal():
         per = srv.run(arrivals, lengths, seeds, batched=False, realtime=False)
         assert per["completed"] == len(arrivals)
         assert np.array_equal(per["checksum"], want)
+        piped = srv.run(arrivals, lengths, seeds, batched=True, realtime=False, pipelined=True)
+        assert piped["completed"] == len(arrivals)
+        assert np.array_equal(piped["checksum"], want)
         for i in (0, 5, 17):
             alone = srv.run(arrivals[i:i + 1], lengths[i:i + 1], seeds[i:i + 1], batched=True, realtime=False)
             assert alone["checksum"][0] == want[i]
@@ -39,7 +42,8 @@ def test_mix_and_alone_checksums_equal():
         assert alloc.error_flags() == 0
 
 
-def test_admission_waits_for_free_chunks():
+@pytest.mark.parametrize("pipelined", [False, True])
+def test_admission_waits_for_free_chunks(pipelined):
     """A heap too small for all requests at once: admission must hold requests
     back until completions return chunks, and every request still completes."""
     from mallocmc_gb300.serve import Server, expected_checksum, make_requests
@@ -48,7 +52,7 @@ def test_admission_waits_for_free_chunks():
     want = np.array([expected_checksum(int(s), int(n)) for s, n in zip(seeds, lengths)], dtype=np.uint64)
     with gpu_allocator(HeapConfig(65536, 8 << 20, 16, 2, False), 16 << 20) as alloc:
         srv = Server(alloc, slots=64, max_chunks=128, step=256, queue_cap=128)
-        res = srv.run(arrivals, lengths, seeds, batched=True, realtime=False)
+        res = srv.run(arrivals, lengths, seeds, batched=True, realtime=False, pipelined=pipelined)
         assert res["completed"] == len(arrivals)
         assert np.array_equal(res["checksum"], want)
         # never more chunks promised than the heap held: some requests had to wait

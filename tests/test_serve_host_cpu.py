@@ -11,7 +11,8 @@ import numpy as np
 import pytest
 
 from mallocmc_gb300 import _lib as L
-from mallocmc_gb300.serve import CMD_DTYPE, ELEMS_PER_CHUNK, SLOT_DTYPE, Server, expected_checksum, make_requests
+from mallocmc_gb300.serve import (CMD_DTYPE, DONE_DTYPE, ELEMS_PER_CHUNK, SLOT_DTYPE, Server, expected_checksum,
+                                  make_requests)
 
 
 class ModelServer(Server):
@@ -27,10 +28,39 @@ class ModelServer(Server):
         self.grow_failures = 0
         self.ticks_seen = 0
         self.max_live = 0
+        self._pipe = []
+        for _ in (0, 1):
+            queue = np.zeros(queue_cap, dtype=CMD_DTYPE)
+            done = np.zeros(slots, dtype=DONE_DTYPE)
+            self._pipe.append({"queue": queue, "q": {f: queue[f] for f in CMD_DTYPE.names},
+                               "qlen": np.zeros(1, np.uint32), "done": done, "done_slot": done["slot"],
+                               "done_checksum": done["checksum"], "done_len": np.zeros(1, np.uint32),
+                               "remaining": np.zeros(1, np.uint64), "free": np.zeros(1, np.uint32)})
+
+    def launch(self, b):
+        """The pipelined tick, run at once: the host only reads its results two
+        ticks later, as it would while the tick ran on the device."""
+        p = self._pipe[b]
+        completed = self._tick(p["queue"], int(p["qlen"][0]))
+        p["done_len"][0] = len(completed)
+        for j, w in enumerate(completed):
+            p["done"][j] = (w, 0, self.slots[w]["checksum"])
+        live = self.slots["state"] == L.MMC_SERVE_LIVE
+        p["remaining"][0] = int((-(-self.slots["final_len"][live].astype(np.int64) // ELEMS_PER_CHUNK)
+                                 - self.slots["nchunks"][live]).sum())
+        p["free"][0] = self.pool
+
+    def wait(self):
+        pass
 
     def tick(self, batched=True):
+        self._tick(self.queue, int(self.queue_len[0]))
+        self.free_chunks[0] = self.pool
+
+    def _tick(self, queue, qlen):
         self.ticks_seen += 1
-        for c in self.queue[: int(self.queue_len[0])]:
+        completed = []
+        for c in queue[:qlen]:
             s = self.slots[c["slot"]]
             if c["kind"] == 1:
                 assert s["state"] == L.MMC_SERVE_FREE, "admitted into a slot that was not released"
@@ -59,18 +89,20 @@ class ModelServer(Server):
                     s["checksum"] = expected_checksum(int(s["seed"]), end)
                     s["state"] = L.MMC_SERVE_DONE
                     self.pool += chunks
+                    completed.append(int(w))
             self.slots[w] = s
-        self.free_chunks[0] = self.pool
+        return completed
 
     def close(self):
         pass
 
 
+@pytest.mark.parametrize("pipelined", [False, True])
 @pytest.mark.parametrize("pool,slots", [(10_000, 16), (40, 16), (16, 64)])
-def test_admission_never_overcommits_and_every_request_completes(pool, slots):
+def test_admission_never_overcommits_and_every_request_completes(pool, slots, pipelined):
     arrivals, lengths, seeds = make_requests(60, rate=1e9, seed=3, median=1024, sigma=1.0, cap=4096)
     srv = ModelServer(pool, slots=slots)
-    res = srv.run(arrivals, lengths, seeds, batched=True, realtime=False)
+    res = srv.run(arrivals, lengths, seeds, batched=True, realtime=False, pipelined=pipelined)
     assert res["completed"] == len(arrivals)
     want = np.array([expected_checksum(int(s), int(n)) for s, n in zip(seeds, lengths)], dtype=np.uint64)
     assert np.array_equal(res["checksum"], want)
@@ -81,11 +113,12 @@ def test_admission_never_overcommits_and_every_request_completes(pool, slots):
     assert srv.max_live <= slots
 
 
-def test_small_pool_holds_requests_back():
+@pytest.mark.parametrize("pipelined", [False, True])
+def test_small_pool_holds_requests_back(pipelined):
     arrivals, lengths, seeds = make_requests(30, rate=1e9, seed=4, median=2048, sigma=0.2, cap=4096)
     need = -(-lengths // ELEMS_PER_CHUNK)
     srv = ModelServer(int(need.max()), slots=16)
-    res = srv.run(arrivals, lengths, seeds, batched=True, realtime=False)
+    res = srv.run(arrivals, lengths, seeds, batched=True, realtime=False, pipelined=pipelined)
     assert res["completed"] == len(arrivals)
     # the pool holds one largest request: never more live than the smallest needs fit
     assert srv.max_live <= int(need.max()) // int(need.min())
@@ -93,10 +126,11 @@ def test_small_pool_holds_requests_back():
     assert srv.grow_failures == 0
 
 
-def test_cut_short_run_drains():
+@pytest.mark.parametrize("pipelined", [False, True])
+def test_cut_short_run_drains(pipelined):
     arrivals, lengths, seeds = make_requests(40, rate=1e9, seed=5, median=4096, sigma=0.1, cap=8192)
     srv = ModelServer(10_000, slots=32, step=16)
-    first = srv.run(arrivals, lengths, seeds, batched=True, realtime=False, max_seconds=0.0)
+    first = srv.run(arrivals, lengths, seeds, batched=True, realtime=False, max_seconds=0.0, pipelined=pipelined)
     assert first["completed"] < len(arrivals)
     assert not (srv.slots["state"] != L.MMC_SERVE_FREE).any()
     assert srv.pool == 10_000
