@@ -437,6 +437,8 @@ mmc_status mmc_serve_pipeline(mmc_server* server, int buffer, mmc_serve_cmd** qu
 mmc_status mmc_serve_launch(mmc_server* server, int buffer);
 /* Wait for every tick launched so far. */
 mmc_status mmc_serve_wait(mmc_server* server);
+/* Wait for the last tick launched on `buffer` (ticks run in launch order). */
+mmc_status mmc_serve_wait_buffer(mmc_server* server, int buffer);
 mmc_status mmc_serve_destroy(mmc_server* server);
 
 /* Relaxed device-scope atomicOr throughput over `words` u32 words at `buf`

@@ -115,6 +115,7 @@ SIGNATURES = {
     "mmc_serve_pipeline": (ctypes.c_int, [vp, ctypes.c_int] + [ctypes.POINTER(vp)] * 6),
     "mmc_serve_launch": (ctypes.c_int, [vp, ctypes.c_int]),
     "mmc_serve_wait": (ctypes.c_int, [vp]),
+    "mmc_serve_wait_buffer": (ctypes.c_int, [vp, ctypes.c_int]),
     "mmc_serve_destroy": (ctypes.c_int, [vp]),
     "mmc_run_fill": (ctypes.c_int, [vp, ctypes.POINTER(MmcFragParams), vp, vp, u64, vp, vp]),
     "mmc_run_free_list": (ctypes.c_int, [vp, vp, vp, vp, u64, vp, vp]),

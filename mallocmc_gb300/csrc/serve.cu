@@ -94,6 +94,7 @@ struct mmc_server
         unsigned long long* d_counts; /* [0]: completions, [1]: chunks still to take */
         cudaGraph_t graph;
         cudaGraphExec_t exec;
+        cudaEvent_t finished; /* recorded after each launch of this buffer's tick */
     } pipe[2];
 };
 
@@ -283,6 +284,8 @@ namespace
                 cudaGraphExecDestroy(p.exec);
             if(p.graph)
                 cudaGraphDestroy(p.graph);
+            if(p.finished)
+                cudaEventDestroy(p.finished);
             cudaFreeHost(p.h_queue);
             cudaFreeHost(p.h_queue_len);
             cudaFreeHost(p.h_done);
@@ -448,6 +451,8 @@ mmc_status mmc_serve_create(mmc_heap* heap, uint32_t slots, uint32_t max_chunks,
         }
         if(st == MMC_OK)
             st = cuda_check(cudaGraphInstantiate(&p.exec, p.graph, 0), "instantiate pipelined tick graph");
+        if(st == MMC_OK)
+            st = cuda_check(cudaEventCreateWithFlags(&p.finished, cudaEventDisableTiming), "tick event");
     }
     if(st != MMC_OK)
     {
@@ -484,7 +489,17 @@ mmc_status mmc_serve_launch(mmc_server* s, int buffer)
 {
     if(s == nullptr || buffer < 0 || buffer > 1)
         return fail(MMC_ERR_ARG, "server is null or buffer not 0 or 1");
-    return cuda_check(cudaGraphLaunch(s->pipe[buffer].exec, s->stream), "pipelined tick launch");
+    mmc_status st = cuda_check(cudaGraphLaunch(s->pipe[buffer].exec, s->stream), "pipelined tick launch");
+    if(st == MMC_OK)
+        st = cuda_check(cudaEventRecord(s->pipe[buffer].finished, s->stream), "record tick event");
+    return st;
+}
+
+mmc_status mmc_serve_wait_buffer(mmc_server* s, int buffer)
+{
+    if(s == nullptr || buffer < 0 || buffer > 1)
+        return fail(MMC_ERR_ARG, "server is null or buffer not 0 or 1");
+    return cuda_check(cudaEventSynchronize(s->pipe[buffer].finished), "wait for tick");
 }
 
 mmc_status mmc_serve_wait(mmc_server* s)

@@ -95,6 +95,9 @@ class Server:
     def wait(self):
         L.check(L.lib().mmc_serve_wait(self._s), "serve_wait")
 
+    def wait_buffer(self, buffer: int):
+        L.check(L.lib().mmc_serve_wait_buffer(self._s, buffer), "serve_wait_buffer")
+
     def close(self):
         if getattr(self, "_s", None):
             L.lib().mmc_serve_destroy(self._s)
@@ -109,9 +112,11 @@ class Server:
     def run_pipelined(self, arrivals, lengths, seeds, realtime: bool = True, max_seconds: float = 60.0):
         """run() with batched ticks in flight while the host works: tick i runs on
         buffer i % 2 with the queue the host built during tick i - 1, from the
-        results tick i - 2 published in the same buffer. The host therefore
-        never reads what a running tick writes, and a tick's period is the
-        longer of the device's and the host's work instead of their sum.
+        results tick i - 2 published in the same buffer; it is queued behind
+        tick i - 1 before the host waits for that one, so the device runs tick
+        after tick without a gap. The host never reads what a running tick
+        writes, and a tick's period is the longer of the device's and the
+        host's work instead of their sum.
         Admission counts against the free chunks of tick i - 2, less the chunks
         its live requests will yet take and the needs admitted in the queue of
         the tick in flight (completions of the tick in flight are not yet
@@ -188,8 +193,10 @@ class Server:
                 cmds += k
                 w_lo += k
             pb["qlen"][0] = cmds
-            self.wait()  # tick i - 1
+            # queue tick i behind tick i - 1 (no gap on the device), then wait
+            # for tick i - 1, whose buffer the next pass reads and rewrites
             self.launch(i & 1)
+            self.wait_buffer((i - 1) & 1)
             ticks += 1
             i += 1
             inflight_pending = pending

@@ -53,6 +53,9 @@ class ModelServer(Server):
     def wait(self):
         pass
 
+    def wait_buffer(self, b):
+        pass
+
     def tick(self, batched=True):
         self._tick(self.queue, int(self.queue_len[0]))
         self.free_chunks[0] = self.pool
