@@ -394,8 +394,10 @@ def serving_column(torch, args, atom_peak=None):
     """Continuous batching on a 64 GiB device-resident heap (pagesize 64 KiB, so a
     16 KiB chunk is a plain chunk): Poisson arrivals at each rate, lognormal
     lengths (median 1024, sigma 1, cap 32768 elements of 2 B), one 16 KiB chunk per
-    256 elements, admission by the free-chunk count; one graph launch per tick
-    against one launch per live request per tick. Latency = admit to completion."""
+    256 elements, admission by the free-chunk count. Three forms: pipelined graph
+    ticks (the host prepares tick i + 1 while tick i runs), synchronous graph
+    ticks, and one launch per live request per tick. Latency = admit to
+    completion."""
     from mallocmc_gb300 import AlignmentPolicies, Allocator, CreationPolicies, DistributionPolicies
     from mallocmc_gb300.serve import Server, expected_checksum, make_requests
 
