@@ -426,6 +426,10 @@ def serving_column(torch, args, atom_peak=None):
                          "throughput_req_per_s": ok.sum() / span if ok.any() else 0.0,
                          "chunks_per_s": float((-(-lengths[ok] // 256)).sum() / span) if ok.any() else 0.0,
                          "ticks": res["ticks"]})
+            if "wait_seconds" in res:
+                # the share of the run the host spent blocked on the device: near 1
+                # when the device's tick is the longer side, near 0 when the host's is
+                rows[-1]["host_blocked_share"] = res["wait_seconds"] / max(res["seconds"], 1e-9)
             if atom_peak:
                 # a 16 KiB chunk on a 64 KiB page: malloc 3 atomics, free 2 (reference algorithm)
                 rows[-1]["atomic_frac"] = rows[-1]["chunks_per_s"] * 5 / atom_peak

@@ -145,6 +145,7 @@ class Server:
         inflight_pending = 0
         released_inflight = []
         i = 0
+        waited = 0.0  # host time blocked on the device
         t0 = time.perf_counter()
         while done < n:
             now = time.perf_counter() - t0
@@ -196,7 +197,9 @@ class Server:
             # queue tick i behind tick i - 1 (no gap on the device), then wait
             # for tick i - 1, whose buffer the next pass reads and rewrites
             self.launch(i & 1)
+            tw = time.perf_counter()
             self.wait_buffer((i - 1) & 1)
+            waited += time.perf_counter() - tw
             ticks += 1
             i += 1
             inflight_pending = pending
@@ -206,7 +209,7 @@ class Server:
         if done < n:
             self._drain(slot_req)
         return {"admit": admit_t, "done": done_t, "checksum": checksum, "ticks": ticks, "seconds": seconds,
-                "completed": done}
+                "completed": done, "wait_seconds": waited}
 
     def run(self, arrivals, lengths, seeds, batched: bool = True, realtime: bool = True, max_seconds: float = 60.0,
             pipelined: bool = False):
