@@ -139,3 +139,12 @@ def test_cut_short_run_drains(pipelined):
     assert srv.pool == 10_000
     again = srv.run(arrivals, lengths, seeds, batched=True, realtime=False)
     assert again["completed"] == len(arrivals)
+
+
+def test_pipelined_ticks_need_room_to_release_every_slot():
+    """A pipelined tick may release every slot at once: a queue shorter than the
+    slot table is refused up front instead of overflowing."""
+    arrivals, lengths, seeds = make_requests(4, rate=1e9, seed=6)
+    srv = ModelServer(1000, slots=64, queue_cap=32)
+    with pytest.raises(ValueError):
+        srv.run(arrivals, lengths, seeds, batched=True, realtime=False, pipelined=True)
