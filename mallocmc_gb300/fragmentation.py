@@ -22,6 +22,23 @@ def frag_params(blocks, threads_per_block, seed, first_request=0, small=(16, 204
     return p
 
 
+def algorithmic_atomics(sizes, freed, pagesize: int) -> int:
+    """Minimum global atomics of a fragmentation run's operations under the
+    reference algorithm, for the successful mallocs of `sizes` and the frees of
+    the entries `freed` indexes: a chunked malloc 3 (CAS chunk size, add count,
+    or mask), a k-page malloc k CASes and the hint CAS; a chunked free 2 (3 on a
+    hierarchical chunk, whose on-page mask is cleared too), a k-page free k
+    CASes and the hint max. A malloc that fails is counted with none."""
+    sizes = np.asarray(sizes, dtype=np.int64)
+    freed = np.asarray(freed, dtype=np.int64)
+    pages = -(-sizes // pagesize)
+    atomics = int(np.where(sizes <= pagesize, 3, pages + 1).sum())
+    fs = sizes[freed[freed < len(sizes)]]
+    ht = (pagesize - 8) // 33
+    atomics += int(np.where(fs <= pagesize, np.where(fs <= ht, 3, 2), -(-fs // pagesize) + 1).sum())
+    return atomics
+
+
 def run_fragmentation(alloc: Allocator, seed: int, blocks: int, threads_per_block: int = 256,
                       capacity: int = 1 << 22, small=(16, 2048), large=(8192, 1 << 20), large_permille=100,
                       stream=None, waves_per_call: int = 8, max_waves: int = 1 << 20, release: bool = False) -> dict:
@@ -81,17 +98,8 @@ def run_fragmentation(alloc: Allocator, seed: int, blocks: int, threads_per_bloc
     torch.cuda.synchronize(dev)
     c = ctr.cpu().numpy().view(np.uint64)
     ops = req_total + len(half)
-    # minimum global atomics of these operations under the reference algorithm:
-    # chunked malloc 3 (CAS chunk size, add count, or mask), k-page malloc k CASes
-    # + the hint CAS; chunked free 2 (3 on a hierarchical chunk), k-page free k
-    # CASes + the hint max; a failing malloc none
-    pagesize = int(alloc.getAllocatorHandle().pagesize)
     got = sizes[: min(n_total, capacity)].cpu().numpy().astype(np.int64)
-    pages = -(-got // pagesize)
-    atomics = int(np.where(got <= pagesize, 3, pages + 1).sum())
-    fs = got[half[half < len(got)]]
-    ht = (pagesize - 8) // 33
-    atomics += int(np.where(fs <= pagesize, np.where(fs <= ht, 3, 2), -(-fs // pagesize) + 1).sum())
+    atomics = algorithmic_atomics(got, half, int(alloc.getAllocatorHandle().pagesize))
     out.update(freed=len(half), phase2_allocs=n_total - n1, final_live_bytes=live2, final_fill=live2 / heap_bytes,
                algorithmic_atomics=atomics, atomics_per_second=atomics / (t1 + tf + t2),
                tag_errors=int(c[3]), free_seconds=tf, phase2_seconds=t2,

@@ -46,3 +46,16 @@ def test_batched_model_counts_the_jobs_pairs():
     w = bench.batched_algorithmic_atomics(jobs, 16384)
     assert w["pairs"] == int(expected_pairs(jobs).sum())
     assert 1.0 < w["atomics_per_pair"] < 7.0
+
+
+def test_fragmentation_atomics_by_operation():
+    """The fragmentation run's atomic count, operation by operation: 4 KiB
+    pages, hierarchical chunks up to (4096 - 8) // 33 = 123 bytes."""
+    from mallocmc_gb300.fragmentation import algorithmic_atomics
+
+    sizes = [64, 2048, 4096, 8192, 12289]  # hierarchical, chunk, whole page, 2 pages, 4 pages
+    assert algorithmic_atomics(sizes, [], 4096) == 3 + 3 + 3 + (2 + 1) + (4 + 1)
+    # frees: 64 B (hierarchical: 3), 4096 B (a chunk of the page size: 2), the 4-page run (4 + 1)
+    assert algorithmic_atomics(sizes, [0, 2, 4], 4096) == 17 + 3 + 2 + 5
+    # an index past the successful mallocs is ignored
+    assert algorithmic_atomics(sizes, [99], 4096) == 17
