@@ -66,6 +66,39 @@ namespace
         mallocMC::ReservePoolPolicies::CudaSetLimits,
         mallocMC::AlignmentPolicies::Noop>;
 
+    /* The reference's policy matrix (tests/policies.cpp:83-187): Scatter or
+     * OldMalloc x XMallocSIMD or Noop x Shrink or Noop, each with its reserve
+     * pool and ReturnNull; there one thread mallocs 4000 bytes and frees them. */
+    template<class Creation, class Distribution, class ReservePool, class Alignment>
+    using PolicyAllocator = mallocMC::Allocator<Acc, Creation, Distribution, mallocMC::OOMPolicies::ReturnNull,
+                                                ReservePool, Alignment>;
+    using Sc = mallocMC::CreationPolicies::Scatter<ScatterHeapConfig, ScatterHashConfig>;
+    using Om = mallocMC::CreationPolicies::OldMalloc;
+    using Xm = mallocMC::DistributionPolicies::XMallocSIMD<>;
+    using Nd = mallocMC::DistributionPolicies::Noop;
+    using Ab = mallocMC::ReservePoolPolicies::AlpakaBuf<Acc>;
+    using Cl = mallocMC::ReservePoolPolicies::CudaSetLimits;
+    using Sh = mallocMC::AlignmentPolicies::Shrink<ShrinkConfig>;
+    using Na = mallocMC::AlignmentPolicies::Noop;
+
+    template<class A>
+    __global__ void policyMatrixKernel(typename A::AllocatorHandle h, int* ok)
+    {
+        const Acc acc{};
+        void* p = h.malloc(acc, 4000);
+        if(p != nullptr)
+        {
+            h.free(acc, p);
+            *ok = 1;
+        }
+    }
+
+    template<class A>
+    std::string policy_info()
+    {
+        return A::info("\n");
+    }
+
     __global__ void oldMallocKernel(OldAllocator::AllocatorHandle h, int length, unsigned long long* sums, int* fails)
     {
         const Acc acc{};
@@ -301,6 +334,40 @@ int mmcx_oldmalloc(int device, int length, unsigned long long* sum, unsigned lon
 }
 
 /* info() strings of the two allocator types (host only). */
+/* The info() strings of the eight allocators of the reference's policy matrix,
+ * separated by "--" lines (host only). */
+int mmcx_policy_matrix_info(char* buf, size_t len)
+{
+    const std::string s = policy_info<PolicyAllocator<Sc, Xm, Ab, Sh>>() + "--\n"
+                          + policy_info<PolicyAllocator<Sc, Xm, Ab, Na>>() + "--\n"
+                          + policy_info<PolicyAllocator<Sc, Nd, Ab, Sh>>() + "--\n"
+                          + policy_info<PolicyAllocator<Sc, Nd, Ab, Na>>() + "--\n"
+                          + policy_info<PolicyAllocator<Om, Xm, Cl, Sh>>() + "--\n"
+                          + policy_info<PolicyAllocator<Om, Xm, Cl, Na>>() + "--\n"
+                          + policy_info<PolicyAllocator<Om, Nd, Cl, Sh>>() + "--\n"
+                          + policy_info<PolicyAllocator<Om, Nd, Cl, Na>>();
+    if(buf == nullptr || len == 0)
+        return 1;
+    std::snprintf(buf, len, "%s", s.c_str());
+    return s.size() < len ? 0 : 1;
+}
+
+/* The device code of the same eight allocators, compiled: the host entry of
+ * each one's malloc(4000)/free kernel (i in 0..7, in the order above). */
+const void* mmcx_policy_matrix_kernel(int i)
+{
+    static const void* const k[8] = {
+        reinterpret_cast<const void*>(&policyMatrixKernel<PolicyAllocator<Sc, Xm, Ab, Sh>>),
+        reinterpret_cast<const void*>(&policyMatrixKernel<PolicyAllocator<Sc, Xm, Ab, Na>>),
+        reinterpret_cast<const void*>(&policyMatrixKernel<PolicyAllocator<Sc, Nd, Ab, Sh>>),
+        reinterpret_cast<const void*>(&policyMatrixKernel<PolicyAllocator<Sc, Nd, Ab, Na>>),
+        reinterpret_cast<const void*>(&policyMatrixKernel<PolicyAllocator<Om, Xm, Cl, Sh>>),
+        reinterpret_cast<const void*>(&policyMatrixKernel<PolicyAllocator<Om, Xm, Cl, Na>>),
+        reinterpret_cast<const void*>(&policyMatrixKernel<PolicyAllocator<Om, Nd, Cl, Sh>>),
+        reinterpret_cast<const void*>(&policyMatrixKernel<PolicyAllocator<Om, Nd, Cl, Na>>)};
+    return (i >= 0 && i < 8) ? k[i] : nullptr;
+}
+
 int mmcx_info(char* buf, size_t len)
 {
     const std::string s = ScatterAllocator::info("\n") + "--\n" + DefaultAllocator::info("\n");

@@ -26,6 +26,9 @@ def ex():
                                  ctypes.POINTER(ctypes.c_ulonglong), ctypes.POINTER(ctypes.c_uint),
                                  ctypes.POINTER(ctypes.c_int)]
     L.mmcx_info.argtypes = [ctypes.c_char_p, ctypes.c_size_t]
+    L.mmcx_policy_matrix_info.argtypes = [ctypes.c_char_p, ctypes.c_size_t]
+    L.mmcx_policy_matrix_kernel.argtypes = [ctypes.c_int]
+    L.mmcx_policy_matrix_kernel.restype = ctypes.c_void_p
     return L
 
 
@@ -37,6 +40,28 @@ def test_info_strings(ex):
     assert "HierarchyThreshold=123" in s and "minChunkSize=3" in s
     assert "DistributionPolicy:  XMallocSIMD[4096]" in s and "DistributionPolicy:  Noop" in s
     assert "AlignmentPolicy:     Shrink[16]" in s and "OOMPolicy:           ReturnNull" in s
+
+
+def test_policy_matrix_compiles(ex):
+    """The reference's policy matrix (tests/policies.cpp:83-187): every
+    combination of Scatter/OldMalloc, XMallocSIMD/Noop distribution and
+    Shrink/Noop alignment names its policies and has its device code built."""
+    buf = ctypes.create_string_buffer(16384)
+    assert ex.mmcx_policy_matrix_info(buf, len(buf)) == 0
+    blocks = buf.value.decode().split("--\n")
+    assert len(blocks) == 8
+    want = [(c, d, r, a) for c, r in (("Scatter[", "AlpakaBuf"), ("OldMalloc", "CudaSetLimits"))
+            for d in ("XMallocSIMD[", "Noop") for a in ("Shrink[", "Noop")]
+    for b, (c, d, r, a) in zip(blocks, want):
+        lines = dict(line.split(":", 1) for line in b.strip().splitlines())
+        assert lines["CreationPolicy"].strip().startswith(c)
+        assert lines["DistributionPolicy"].strip().startswith(d)
+        assert lines["ReservePoolPolicy"].strip() == r
+        assert lines["AlignmentPolicy"].strip().startswith(a)
+        assert lines["OOMPolicy"].strip() == "ReturnNull"
+    kernels = [ex.mmcx_policy_matrix_kernel(i) for i in range(8)]
+    assert all(kernels) and len(set(kernels)) == 8
+    assert ex.mmcx_policy_matrix_kernel(8) is None
 
 
 def test_reference_example_config_is_rejected(ex):
