@@ -11,8 +11,11 @@ uniform in {16, 32, ..., 1024}, drawn from a seeded SplitMix64 table
   e2e              pairs/s through the C ABI with host buffers: H2D of each step's size
                    table from pinned memory (pipelined on a copy stream) + kernel + D2H
                    of the result counters, over the whole span
-  roofline         HBM roofline of the stress kernel (payload + metadata bytes)
-  atomic_roofline  L2 atomic ops/s against a measured atomicOr peak
+  roofline         L2 atomic roofline of the stress kernel: the reference algorithm's
+                   minimum atomics per pair x pairs / kernel time, against the atomicOr
+                   rate measured in the same run (and against the non-returning `red` rate)
+  hbm_roofline     the kernel's DRAM traffic (ncu) / kernel time against measured HBM
+  l2_bytes         the workload's SM<->L2 bytes (payload written and read back + metadata)
   oldmalloc        the same stress on CUDA's device heap (CreationPolicies::OldMalloc)
   batched          uneven jobs in one graph-captured persistent launch vs one launch per job,
                    with its own atomic roofline (the reference algorithm's atomics for
@@ -21,11 +24,15 @@ uniform in {16, 32, ..., 1024}, drawn from a seeded SplitMix64 table
                    (and each row's atomic fraction)
   fragmentation    fill at out-of-memory against the oracle's serial run (and the run's
                    atomic fraction)
-  cpu_baseline     the oracle port of the reference's CPU backend on the host cores
+  cpu_baseline     the reference's own CPU backends on the host cores: the unmodified
+                   reference headers on alpaka AccCpuOmp2Blocks (every host core) and
+                   AccCpuSerial (one core), the faster reported (oracle/ref_stress.cpp),
+                   beside the oracle port (oracle/scatter_oracle.c)
 
-`--impl reference` times the reference's CPU implementation of the path (the
-oracle port of its CPU backend, oracle/scatter_oracle.c) on the host cores instead.
-Multi-GPU: replicas only (each rank owns an independent heap).
+`--impl reference` times the same reference CPU backends (the oracle port where
+the reference headers are not installed under baseline/_ref) on the host cores.
+Multi-GPU: replicas only (each rank owns an independent heap); `--gpus N`
+without a launcher starts N ranks under torch.distributed.run itself.
 """
 from __future__ import annotations
 
@@ -68,7 +75,10 @@ def parse():
     ap.add_argument("--pattern", default="warp", choices=["warp", "thread"],
                     help="how each block is written and verified: by its warp, 512 B per instruction, or by its thread")
     ap.add_argument("--oldmalloc-rounds", type=int, default=10, help="rounds of the CUDA device-malloc comparison")
-    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target length of the CPU baseline sample")
+    ap.add_argument("--cpu-seconds", type=float, default=4.0,
+                    help="target length of each CPU baseline step (reference backends and oracle port)")
+    ap.add_argument("--ref-step-seconds", type=float, default=1.5,
+                    help="target length of each step of the reference arm (--impl reference)")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--no-frag", action="store_true")
@@ -308,7 +318,7 @@ def oldmalloc_column(torch, stream, heap_bytes, blocks, tpb, rounds, d_sizes, fl
             "rounds": rounds, "ms_per_launch": statistics.median(ms), "nulls": int(st[1]), "pattern_errors": int(st[2])}
 
 
-def batched_column(torch, args, sms, atom_peak=None):
+def batched_column(torch, args, sms, atom_peak=None, red_peak=None):
     """512 uneven jobs on one 16 GiB heap: one persistent graph-captured launch
     against one plain launch per job (same allocations, checked job by job).
     With atom_peak (measured L2 atomics/s), each form's algorithmic atomics per
@@ -370,6 +380,8 @@ def batched_column(torch, args, sms, atom_peak=None):
         ach = w["atomics"] / (ms * 1e-3)
         out = {"bound": "l2_atomic", "achieved": ach / 1e9, "peak": atom_peak / 1e9, "unit": "Gatomic/s",
                "frac": ach / atom_peak, "atomics_per_pair": w["atomics_per_pair"], "form": "graph"}
+        if red_peak:
+            out["frac_vs_red_peak"] = ach / red_peak
         if c == GB300_TUNED:
             out["ncu_atomics_per_pair"] = BATCH_NCU_ATOMICS_PER_PAIR
             out["ncu_frac"] = pairs / (ms * 1e-3) * BATCH_NCU_ATOMICS_PER_PAIR / atom_peak
@@ -491,6 +503,28 @@ def fragmentation_column(torch, args, sms, atom_peak=None):
             "reference": ref, **runs}
 
 
+def host_cores() -> int:
+    """Host threads this process may run on (the cgroup/affinity set, not the machine's count)."""
+    try:
+        return len(os.sched_getaffinity(0))
+    except (AttributeError, OSError):
+        return os.cpu_count() or 1
+
+
+def cpu_model() -> str:
+    """The host CPU's model name (lscpu), for the baseline's description."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.strip().lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    import platform
+
+    return platform.machine()
+
+
 def cpu_port_run(heap_gib, accessblock_mib, threads_total, rounds, target_s, workers):
     """The oracle port of the reference's CPU backend on `workers` host threads,
     on a bounded sample (virtual threads x rounds) of the same workload and
@@ -511,6 +545,78 @@ def cpu_port_run(heap_gib, accessblock_mib, threads_total, rounds, target_s, wor
         total["steps"] += 1
     heap.close()
     return total, vthreads
+
+
+# The reference's own CPU backends (alpaka AccCpuOmp2Blocks on all host cores,
+# AccCpuSerial on one) running the stress through the unmodified reference
+# headers: oracle/ref_stress.cpp, built by oracle/Makefile from the reference's
+# headers installed under baseline/_ref (`make -C oracle install-ref REF=...`).
+REF_INSTALL = os.path.join(ROOT, "baseline", "_ref")
+REF_STRESS = {"omp": os.path.join(ROOT, "oracle", "_ref", "ref_stress_omp"),
+              "serial": os.path.join(ROOT, "oracle", "_ref", "ref_stress_serial")}
+REF_STRESS_CONFIGS = {4096: "p4k_ab4g_r16_w2", 2048: "p4k_ab2g_r16_w2", 8: "p4k_ab8m_r16_w2"}
+
+
+def ensure_ref_stress():
+    """Build the reference stress binaries if they are missing. Returns None when
+    they are ready, else the reason they cannot be built."""
+    if all(os.access(b, os.X_OK) for b in REF_STRESS.values()):
+        return None
+    src = os.environ.get("MALLOCMC_REFERENCE") or REF_INSTALL
+    if not os.path.isdir(os.path.join(src, "src", "include", "mallocMC")):
+        return f"reference headers not installed under {os.path.relpath(src, ROOT)}"
+    r = subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "ref-stress", f"REF={src}"],
+                       capture_output=True, text=True)
+    if r.returncode != 0:
+        return "reference stress build failed: " + (r.stderr.strip().splitlines() or ["?"])[-1]
+    return None
+
+
+def ref_stress_run(backend, accessblock_mib, heap_bytes, threads_total, rounds, warmup, steps, target_s, workers):
+    """Run the reference's stress on one alpaka CPU backend ('omp' on `workers`
+    host threads, 'serial' on one): per-step pairs/s over a bounded sample of
+    the workload. Returns the per-step results and the summary line."""
+    cfg = REF_STRESS_CONFIGS.get(accessblock_mib)
+    if cfg is None:
+        raise ValueError(f"no reference configuration for a {accessblock_mib} MiB access block")
+    env = dict(os.environ)
+    if backend == "omp":
+        env["OMP_NUM_THREADS"] = str(workers)
+        env.setdefault("OMP_PROC_BIND", "false")
+    cmd = [REF_STRESS[backend], cfg, str(heap_bytes), str(threads_total), str(rounds), str(SEED), str(warmup),
+           str(steps), f"{target_s:g}"]
+    r = subprocess.run(cmd, capture_output=True, text=True, env=env)
+    if r.returncode != 0:
+        raise RuntimeError(f"reference stress failed ({r.returncode}): {r.stderr.strip()[-400:]}")
+    rows = [json.loads(x) for x in r.stdout.splitlines() if x.startswith("{")]
+    summary = next(x for x in rows if x.get("summary"))
+    per_step = [x for x in rows if "step" in x]
+    if summary["nulls"] or summary["bad"]:
+        raise RuntimeError(f"reference stress reported nulls or pattern errors: {summary}")
+    return per_step, summary
+
+
+def reference_cpu_baseline(args, threads_total, warmup, steps, target_s):
+    """Both alpaka CPU backends of the reference on this host; the faster one
+    is the baseline (on the stress the striped-mutex atomics of the OpenMP
+    backend make all cores slower than one). None, reason if unavailable."""
+    why = ensure_ref_stress()
+    if why is not None:
+        return None, why
+    workers = host_cores()
+    heap_bytes = int(args.heap_gib * (1 << 30))
+    runs = {}
+    for backend in ("omp", "serial"):
+        try:
+            per_step, summ = ref_stress_run(backend, args.accessblock_mib, heap_bytes, threads_total, args.rounds,
+                                            warmup, steps, target_s, workers)
+        except (RuntimeError, ValueError, OSError) as e:
+            return None, str(e)
+        vals = [x["pairs"] / x["seconds"] for x in per_step]
+        runs[backend] = {"value": float(statistics.median(vals)), "per_step": vals, "summary": summ,
+                         "cores": summ["workers"]}
+    best = max(runs, key=lambda b: runs[b]["value"])
+    return {"best": best, "runs": runs, "model": cpu_model()}, None
 
 
 def max_over_ranks(x: float, dist, device) -> float:
@@ -544,45 +650,108 @@ def stress_config(args, sms, world):
             "parallelism": "replicas" if world > 1 else "single GPU"}
 
 
+def sm_count() -> int:
+    """SMs of the GPU this rank would use (152 on GB300 when no GPU is visible)."""
+    try:
+        import torch
+
+        if torch.cuda.is_available():
+            return torch.cuda.get_device_properties(int(os.environ.get("LOCAL_RANK", "0"))).multi_processor_count
+    except Exception:
+        pass
+    return 152
+
+
 def reference_arm(args):
+    """The reference's CPU implementation of the path on the host cores: the
+    unmodified reference headers on alpaka's CPU backends (the faster of
+    AccCpuOmp2Blocks on every host core and AccCpuSerial), or the oracle port
+    of its CPU backend when the reference headers are not installed. Rank 0
+    alone runs; the other ranks exit without work."""
     rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", str(args.gpus)))
     if rank != 0:
         return
-    workers = os.cpu_count() or 1
-    threads_total = 152 * args.blocks_per_sm * args.threads
-    per_step_s = 2.0
-    heap_gib = args.heap_gib
-    try:
-        from oracle.oracle import lib as olib
+    sms = sm_count()
+    threads_total = sms * args.blocks_per_sm * args.threads
+    per_step_s = args.ref_step_seconds
+    ref, why = reference_cpu_baseline(args, threads_total, args.warmup, args.steps, per_step_s)
+    if ref is not None:
+        run = ref["runs"][ref["best"]]
+        v = run["value"]
+        summ = run["summary"]
+        other = "serial" if ref["best"] == "omp" else "omp"
+        cpu = {"value": v, "unit": UNIT, "cores": run["cores"], "kind": "reference",
+               "backend": summ["backend"], "cpu_model": ref["model"],
+               "sample": (f"per step {summ['virtual_threads']} virtual threads x {args.rounds} rounds of the workload "
+                          f"(the unmodified reference headers, {summ['backend']}, {run['cores']} host threads, "
+                          f"heap {args.heap_gib:g} GiB with {args.accessblock_mib} MiB access blocks), about "
+                          f"{per_step_s:g} s"),
+               "other_backend": {"backend": ref["runs"][other]["summary"]["backend"],
+                                 "value": ref["runs"][other]["value"], "cores": ref["runs"][other]["cores"]}}
+        ms = 1e3 * summ["seconds"] / max(1, summ["steps"])
+        errors = {"nulls": summ["nulls"], "pattern": summ["bad"]}
+    else:
+        workers = host_cores()
+        olib_ok = True
+        try:
+            from oracle.oracle import lib as olib
 
-        olib()
-    except Exception:
-        subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "liboracle.so"], check=True, capture_output=True)
-    vals, samples = [], None
-    for i in range(args.warmup + args.steps):
-        r, vt = cpu_port_run(heap_gib, args.accessblock_mib, threads_total, args.rounds, per_step_s, workers)
-        if i >= args.warmup:
-            vals.append(r["pairs"] / r["seconds"])
-            samples = (vt, r)
-    v = float(statistics.median(vals))
-    vt, r = samples
+            olib()
+        except Exception:
+            olib_ok = subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "liboracle.so"],
+                                     capture_output=True).returncode == 0
+        if not olib_ok:
+            print(json.dumps({"impl": "reference", "unavailable": f"{why}; oracle port failed to build"}))
+            return
+        vals, samples = [], None
+        for i in range(args.warmup + args.steps):
+            r, vt = cpu_port_run(args.heap_gib, args.accessblock_mib, threads_total, args.rounds, per_step_s, workers)
+            if i >= args.warmup:
+                vals.append(r["pairs"] / r["seconds"])
+                samples = (vt, r)
+        v = float(statistics.median(vals))
+        vt, r = samples
+        cpu = {"value": v, "unit": UNIT, "cores": workers, "kind": "port", "cpu_model": cpu_model(),
+               "reference_unavailable": why,
+               "sample": f"per step {r['steps']} x ({vt} virtual threads x {args.rounds} rounds) of the workload "
+                         f"(oracle port, alpaka CPU-backend semantics: warp size 1, smid = warpid = 0; same heap "
+                         f"geometry) on {workers} host threads, about {per_step_s:g} s"}
+        ms = 1e3 * r["seconds"]
+        errors = {"nulls": r["nulls"], "pattern": r["bad"]}
     line = {
-        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": 1e3 * r["seconds"], "higher_is_better": True, "scaling": "weak",
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u32", "data": "synthetic (seeded SplitMix64 size draws)",
-        "config": stress_config(args, 152, args.gpus),
-        "cpu_baseline": {"value": v, "unit": UNIT, "cores": workers, "kind": "port",
-                         "sample": f"per step {r['steps']} x ({vt} virtual threads x {args.rounds} rounds) of the "
-                                   f"workload (alpaka CPU-backend semantics: warp size 1, smid = warpid = 0; same heap "
-                                   f"geometry) on {workers} host threads, about {per_step_s:g} s"},
+        "config": stress_config(args, sms, world),
+        "cpu_baseline": cpu,
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        "errors": {"nulls": r["nulls"], "pattern": r["bad"]},
+        "errors": errors,
     }
     print(json.dumps(line))
 
 
+def relaunch_as_ranks(args) -> int:
+    """`--gpus N` (N > 1) without a launcher: start N ranks of this script under
+    torch.distributed.run on this node (one rank per GPU, replicas) and return
+    their exit status."""
+    import socket
+
+    with socket.socket() as sk:
+        sk.bind(("127.0.0.1", 0))
+        port = sk.getsockname()[1]
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", f"--nproc-per-node={args.gpus}",
+           "--master-addr=127.0.0.1", f"--master-port={port}", os.path.abspath(__file__)] + sys.argv[1:]
+    return subprocess.run(cmd).returncode
+
+
 def main():
     args = parse()
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        sys.exit(relaunch_as_ranks(args))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if world != args.gpus:
+        raise SystemExit(f"--gpus {args.gpus} but {world} ranks were launched")
     if args.impl == "reference":
         reference_arm(args)
         return
@@ -591,7 +760,6 @@ def main():
     from mallocmc_gb300 import AlignmentPolicies, Allocator, CreationPolicies, DistributionPolicies, _lib
     from mallocmc_gb300.workloads import launch_stress, stress_params
 
-    world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if not os.path.exists(_lib.LIB_PATH):
@@ -713,26 +881,39 @@ def main():
 
     peaks, peak_kind = measured_peaks()
     kernel_s = per_step_ms * 1e-3
-    achieved_gbs = work["bytes"] / kernel_s / 1e9
-    roofline = {"bound": "hbm", "achieved": achieved_gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                "frac": achieved_gbs / peaks["hbm_gbs"],
-                "traffic": STRESS_DRAM_BYTES_PER_PAIR * work["pairs"], "traffic_note": STRESS_TRAFFIC_NOTE,
-                "peak_kind": peak_kind,
-                "algorithmic_bytes_per_launch": work["bytes"], "payload_bytes_per_launch": work["payload_bytes"],
-                "metadata_bytes_per_launch": work["metadata_bytes"], "kernel": "mmc_stress_kernel"}
-    atomic = None
+    traffic = STRESS_DRAM_BYTES_PER_PAIR * work["pairs"]
+    # DRAM bytes against HBM: the payload stays in L2 (written, read back and
+    # discarded there), so what crosses HBM is the partial end lines and metadata
+    hbm = {"bound": "hbm", "achieved": traffic / kernel_s / 1e9, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+           "frac": traffic / kernel_s / 1e9 / peaks["hbm_gbs"], "traffic": traffic, "traffic_note": STRESS_TRAFFIC_NOTE,
+           "peak_kind": peak_kind, "kernel": "mmc_stress_kernel"}
+    # the workload's algorithmic bytes (payload written and read back + metadata),
+    # which move between the SMs and L2, not DRAM
+    l2_bytes = {"achieved_gbs": work["bytes"] / kernel_s / 1e9, "algorithmic_bytes_per_launch": work["bytes"],
+                "payload_bytes_per_launch": work["payload_bytes"], "metadata_bytes_per_launch": work["metadata_bytes"],
+                "unit": "GB/s", "note": "SM<->L2 bytes of the workload (not DRAM): 2 x payload + metadata"}
+    roofline = dict(hbm)
     pk = None
     if not args.no_peak:
+        # The contract's roofline is the L2 atomic one (the unit this path
+        # exercises): the reference algorithm's minimum atomics per pair x
+        # pairs / kernel time, against the atomicOr rate measured in this run.
         pk = atomic_peak(torch, sms)
         ach = work["atomics"] / kernel_s
-        atomic = {"bound": "l2_atomic", "achieved": ach / 1e9, "peak": pk["atom_l2_32MiB"] / 1e9, "unit": "Gatomic/s",
-                  "frac": ach / pk["atom_l2_32MiB"], "atomics_per_pair": work["atomics_per_pair"],
-                  "ncu_atomics_per_pair": STRESS_NCU_ATOMICS_PER_PAIR,
-                  "ncu_frac": work["pairs"] / kernel_s * STRESS_NCU_ATOMICS_PER_PAIR / pk["atom_l2_32MiB"],
-                  "peaks_measured_gops": {k: v / 1e9 for k, v in pk.items()}}
+        roofline = {"bound": "l2_atomic", "achieved": ach / 1e9, "peak": pk["atom_l2_32MiB"] / 1e9,
+                    "unit": "Gatomic/s", "frac": ach / pk["atom_l2_32MiB"],
+                    "frac_vs_red_peak": ach / pk["red_l2_32MiB"],
+                    "traffic": traffic, "traffic_note": STRESS_TRAFFIC_NOTE,
+                    "peak_kind": "measured in this run: mmc_atomic_peak, returning relaxed atomicOr on random words "
+                                 "of a 32 MiB L2-resident buffer (MEASURED_PEAKS.json has no atomic rate)",
+                    "atomics_per_pair": work["atomics_per_pair"], "atomics_per_launch": work["atomics"],
+                    "ncu_atomics_per_pair": STRESS_NCU_ATOMICS_PER_PAIR,
+                    "ncu_frac": work["pairs"] / kernel_s * STRESS_NCU_ATOMICS_PER_PAIR / pk["atom_l2_32MiB"],
+                    "peaks_measured_gops": {k: v / 1e9 for k, v in pk.items()}, "kernel": "mmc_stress_kernel"}
     batched = None
     if not args.no_batched:
-        batched = batched_column(torch, args, sms, pk["atom_l2_32MiB"] if pk else None)
+        batched = batched_column(torch, args, sms, pk["atom_l2_32MiB"] if pk else None,
+                                 pk["red_l2_32MiB"] if pk else None)
     serving = None
     if not args.no_serve:
         serving = serving_column(torch, args, pk["atom_l2_32MiB"] if pk else None)
@@ -744,17 +925,31 @@ def main():
         oldm = oldmalloc_column(torch, stream, heap_bytes, blocks, tpb, args.oldmalloc_rounds, d_sizes, flush, pattern)
     cpu = None
     if not args.no_cpu_baseline:
-        workers = os.cpu_count() or 1
+        workers = host_cores()
         r, vt = cpu_port_run(args.heap_gib, args.accessblock_mib, nthreads, rounds, args.cpu_seconds, workers)
-        cpu = {"value": r["pairs"] / r["seconds"], "unit": UNIT, "cores": workers, "kind": "port",
-               "sample": f"{r['steps']} x ({vt} virtual threads x {rounds} rounds) (alpaka CPU-backend semantics) "
-                         f"on {workers} host threads, {r['seconds']:.1f} s"}
+        port = {"value": r["pairs"] / r["seconds"], "unit": UNIT, "cores": workers, "kind": "port",
+                "sample": f"{r['steps']} x ({vt} virtual threads x {rounds} rounds) (oracle port, alpaka CPU-backend "
+                          f"semantics) on {workers} host threads, {r['seconds']:.1f} s"}
+        ref, why = reference_cpu_baseline(args, nthreads, 1, 3, args.cpu_seconds)
+        if ref is None:
+            cpu = dict(port, reference_unavailable=why, cpu_model=cpu_model())
+        else:
+            run = ref["runs"][ref["best"]]
+            summ = run["summary"]
+            cpu = {"value": run["value"], "unit": UNIT, "cores": run["cores"], "kind": "reference",
+                   "backend": summ["backend"], "cpu_model": ref["model"],
+                   "sample": (f"3 steps of {summ['virtual_threads']} virtual threads x {rounds} rounds (the unmodified "
+                              f"reference headers on {summ['backend']}, {run['cores']} host threads), "
+                              f"{summ['seconds']:.1f} s"),
+                   "backends": {b: {"value": x["value"], "cores": x["cores"], "backend": x["summary"]["backend"]}
+                                for b, x in ref["runs"].items()},
+                   "port": port}
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": per_step_ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
         "data": "synthetic (seeded SplitMix64 size draws)",
         "config": stress_config(args, sms, world),
-        "roofline": roofline, "atomic_roofline": atomic, "cpu_baseline": cpu, "e2e": e2e,
+        "roofline": roofline, "hbm_roofline": hbm, "l2_bytes": l2_bytes, "cpu_baseline": cpu, "e2e": e2e,
         "oldmalloc": oldm, "batched": batched, "serving": serving, "fragmentation": frag,
         "gpu_launches": args.steps, "clocks": clk.summary(), "wall_s_timed": wall,
         "per_step_ms": ms,

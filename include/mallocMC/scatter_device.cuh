@@ -844,6 +844,7 @@ namespace mmc
             char* pages;
             u32 numpages;
             u32 pagesize;
+            u32 reference_quirks;
         };
 
         /* markpages (Scatter.hpp:745-764) for concurrent callers: the CASes go
@@ -928,7 +929,13 @@ namespace mmc
                                && markpages_batched(c, q, pagestoalloc, bytes, free_below))
                             {
                                 if(!left_free)
-                                    atomicCAS(&c.state->firstFreePageBased, startpage, q - 1u);
+                                {
+                                    /* the reference stores q - 1, which wraps for a run
+                                     * ending at page 0 (Scatter.hpp:800-804) and leaves
+                                     * every later search empty; fixed mode stores 0 */
+                                    const u32 nf = (!c.reference_quirks && q == 0u) ? 0u : q - 1u;
+                                    atomicCAS(&c.state->firstFreePageBased, startpage, nf);
+                                }
                                 return c.pages + static_cast<u64>(q) * c.pagesize;
                             }
                             MMC_STAT(c, MMC_STAT_PAGE_LOST);
@@ -974,7 +981,7 @@ namespace mmc
             if(Ids::warpSize == 1u)
                 return alloc_page_based_single(h, bytes);
             return alloc_page_based_concurrent(
-                PageScan{h.chunksize, h.state, h.pages, h.numpages, h.pagesize}, bytes);
+                PageScan{h.chunksize, h.state, h.pages, h.numpages, h.pagesize, h.reference_quirks}, bytes);
         }
 
         /* deallocPageBased, Scatter.hpp:874-886 (out of line, as the search) */
@@ -1163,14 +1170,28 @@ namespace mmc
         /* For a caller about to free a block whose contents are dead: drop the
          * whole 128-byte lines inside [p, p + bytes) from L2 without writing
          * them back to DRAM (discard.global.L2; their bytes become
-         * indeterminate), then read one word of each line through L2. The
-         * returned pointer equals p but depends on those reads, so a free of
-         * it is issued only after every discard has taken effect in L2 and no
-         * later owner's writes can be discarded. Partial lines at the ends are
-         * left alone (they may hold a neighbouring block). No counterpart in
-         * the reference: a short-lived block's payload otherwise costs a DRAM
-         * write-back after it is freed. */
-        __device__ __forceinline__ void* discard_dead_block(void* p, u32 bytes)
+         * indeterminate), and return p in a form the free must wait for.
+         * Partial lines at the ends are left alone (they may hold a
+         * neighbouring block). No counterpart in the reference: a short-lived
+         * block's payload otherwise costs a DRAM write-back after it is freed.
+         *
+         * Why no later owner's data can be discarded. In the PTX memory model
+         * the discard is a weak write of indeterminate bytes to each line.
+         * After the discards this thread reads one word of every line with a
+         * strong load (ld.relaxed.gpu, which the compiler may neither drop
+         * nor move above the discard it follows: same address, program
+         * order, both asm volatile with a memory clobber). That read is served
+         * by L2 after the discard of its line. The returned pointer is
+         * p + (OR of the words read & runtime_zero): runtime_zero is 0 at run
+         * time but a value the compiler cannot see (a kernel parameter, such
+         * as the handle's `zero` field), so the sum cannot be folded and the
+         * pointer carries a data dependency on every read. The free's first
+         * access (the page's chunk-size load, whose address comes from the
+         * pointer) and every atomic after it therefore issue only once all
+         * reads have returned, i.e. once every discard has taken effect in L2.
+         * A later owner can reach the block only through the free's atomics,
+         * so its writes arrive at L2 after the discards. */
+        __device__ __forceinline__ void* discard_dead_block(void* p, u32 bytes, u32 runtime_zero)
         {
             const u64 a = reinterpret_cast<u64>(p);
             const u64 lo = (a + 127ull) & ~127ull;
@@ -1179,17 +1200,14 @@ namespace mmc
                 asm volatile("discard.global.L2 [%0], 128;" ::"l"(x) : "memory");
             u32 token = 0u;
             for(u64 x = lo; x + 128ull <= end; x += 128ull)
-            {
-                u32 v;
-                asm volatile("ld.global.cg.u32 %0, [%1];" : "=r"(v) : "l"(x) : "memory");
-                token |= v;
-            }
-            void* r;
-            asm volatile("{\n\t.reg .u32 z;\n\t.reg .u64 z64;\n\tand.b32 z, %2, 0;\n\tcvt.u64.u32 z64, z;\n\t"
-                         "add.u64 %0, %1, z64;\n\t}"
-                         : "=l"(r)
-                         : "l"(p), "r"(token));
-            return r;
+                token |= ld_rlx(reinterpret_cast<const u32*>(x));
+            return static_cast<char*>(p) + (token & runtime_zero);
+        }
+
+        /* discard_dead_block with the heap handle's run-time zero. */
+        __device__ __forceinline__ void* discard_dead_block(const mmc_device_handle& h, void* p, u32 bytes)
+        {
+            return discard_dead_block(p, bytes, h.zero);
         }
 
         /* ------------------------------------------------ free-slot counting */

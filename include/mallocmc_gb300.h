@@ -49,6 +49,8 @@ typedef enum mmc_status
 #define MMC_DEVERR_TIMEOUT 0x1u  /* the page-based mutex wait hit its iteration bound */
 #define MMC_DEVERR_BADFREE 0x2u  /* free of a pointer outside the heap or on an unformatted page */
 #define MMC_DEVERR_OOM 0x4u      /* an allocation failed under MMC_OOM_FLAG */
+#define MMC_DEVERR_BADCMD 0x8u   /* a serving tick skipped a command (slot beyond the table, unknown kind)
+                                    or cut a queue length beyond the queue's capacity */
 
 /* Device event counters (mmc_heap_stats); maintained only when the library is
  * built with MMC_DEVICE_STATS, zero otherwise. */
@@ -126,6 +128,9 @@ typedef struct mmc_device_handle
     uint32_t minChunkSize;       /* (pagesize - 128) / 1024 */
     uint32_t paddedMinChunkSize; /* minChunkSize after alignment padding */
     uint32_t maxOnPageMasks;     /* min(32, ceil(pagesize / (32 * minChunkSize + 4))) */
+    uint32_t zero;               /* always 0: a value the compiler cannot know, which
+                                    mmc::dev::discard_dead_block folds into the freed
+                                    pointer to make the free depend on its reads */
 } mmc_device_handle;
 
 typedef struct mmc_heap mmc_heap;
@@ -192,22 +197,25 @@ mmc_status mmc_available_slots(mmc_heap* heap, size_t slot_size, void* stream, u
 mmc_status mmc_available_slots_async(mmc_heap* heap, size_t slot_size, void* stream, unsigned* out_dev);
 
 /* Free-slot count that allocates nothing, for callers that cannot call
- * cudaMalloc: code running while a CUDA graph is being captured (a global-mode
- * capture refuses cudaMalloc), and code inside a framework whose device memory
- * belongs to its own pool allocator, which holds only a device handle and must
- * not take memory behind the pool's back. It needs no mmc_heap, only the
- * handle: the scan's partial sums live in one file-scope __device__ array of
- * MMC_NOALLOC_SCAN_BLOCKS_MAX entries (16 bytes each, 32 KiB in all), which every
- * GPU that loads the library holds until the process exits. The count is
- * written to *out_dev (device memory) when `stream` reaches it.
+ * cudaMalloc: code inside a framework whose device memory belongs to its own
+ * pool allocator, which must not take memory behind the pool's back; a
+ * plugin that is handed only a device handle, with no mmc_heap and so no
+ * heap-owned scratch; a latency-bound host loop (a serving tick, say) that
+ * cannot afford cudaMalloc's implicit device-wide synchronisation. It needs
+ * only the handle: the scan's partial sums live in one file-scope __device__
+ * array of MMC_NOALLOC_SCAN_BLOCKS_MAX entries (16 bytes each, 32 KiB in all),
+ * which every GPU that loads the library holds until the process exits. The
+ * count is written to *out_dev (device memory) when `stream` reaches it.
  * scan_blocks = 0 picks 4 x the SM count; more than MMC_NOALLOC_SCAN_BLOCKS_MAX
  * is rejected with MMC_ERR_ARG. The calling thread's current device must be
  * the heap's. The first call on a device looks up the array's device address
- * (cudaGetSymbolAddress), so make that first call before any stream capture.
- * Every call shares the array: calls that overlap on the GPU (on two streams,
- * say) race and may return wrong counts. Each call rewrites every entry it
- * reads, so nothing carries over from the last call. This entry point has no
- * counterpart in the reference. */
+ * (cudaGetSymbolAddress), so make that first call before any stream capture;
+ * the lookup is repeated on the first call after the device's context changed
+ * (after a cudaDeviceReset, say), which should then also come before any
+ * capture. Every call shares the array: calls that overlap on the GPU (on two
+ * streams, say) race and may return wrong counts. Each call rewrites every
+ * entry it reads, so nothing carries over from the last call. This entry
+ * point has no counterpart in the reference. */
 #define MMC_NOALLOC_SCAN_BLOCKS_MAX 2048
 mmc_status mmc_available_slots_noalloc(const mmc_device_handle* handle, size_t slot_size, unsigned scan_blocks,
                                        void* stream, unsigned* out_dev);
@@ -413,8 +421,17 @@ mmc_status mmc_serve_create(mmc_heap* heap, uint32_t slots, uint32_t max_chunks,
 mmc_status mmc_serve_queue(mmc_server* server, mmc_serve_cmd** queue, uint32_t** queue_len, mmc_serve_slot** slots,
                            unsigned** free_chunks);
 /* Run one tick and wait for it: batched != 0 replays the captured graph (all
- * live requests in one launch); 0 launches one kernel per live request. */
+ * live requests in one launch); 0 launches one kernel per live request. The
+ * queue is checked first (mmc_serve_check_queue): on MMC_ERR_ARG nothing is
+ * launched. The tick's kernels check it again, since the queue is host memory
+ * the caller may change at any time: they cut a length beyond the capacity and
+ * skip a bad command, and set MMC_DEVERR_BADCMD (mmc_heap_error). */
 mmc_status mmc_serve_tick(mmc_server* server, int batched);
+
+/* Host-side check of a command queue before a tick: MMC_ERR_ARG when
+ * queue_len exceeds queue_cap, or a command has a kind other than 1 or 2 or a
+ * slot >= slots. Needs no GPU. */
+mmc_status mmc_serve_check_queue(const mmc_serve_cmd* queue, uint32_t queue_len, uint32_t queue_cap, uint32_t slots);
 
 /* Pipelined ticks: two buffers (b = 0, 1), each with its own command queue and
  * its own results, so the host reads one tick's results and writes the next
@@ -433,7 +450,9 @@ typedef struct mmc_serve_done
 mmc_status mmc_serve_pipeline(mmc_server* server, int buffer, mmc_serve_cmd** queue, uint32_t** queue_len,
                               mmc_serve_done** done, uint32_t** done_len, unsigned long long** remaining,
                               unsigned** free_chunks);
-/* Launch the batched tick on `buffer` without waiting for it. */
+/* Launch the batched tick on `buffer` without waiting for it. Like
+ * mmc_serve_tick, it first checks the buffer's queue (mmc_serve_check_queue)
+ * and launches nothing on MMC_ERR_ARG. */
 mmc_status mmc_serve_launch(mmc_server* server, int buffer);
 /* Wait for every tick launched so far. */
 mmc_status mmc_serve_wait(mmc_server* server);

@@ -14,7 +14,7 @@ LIB_PATH = os.path.join(PKG, "libmallocmc_gb300.so")
 MMC_OK, MMC_ERR_CONFIG, MMC_ERR_CUDA, MMC_ERR_TIMEOUT, MMC_ERR_OOM, MMC_ERR_ARG = range(6)
 MMC_DIST_NOOP, MMC_DIST_XMALLOCSIMD = 0, 1
 MMC_OOM_RETURNNULL, MMC_OOM_FLAG = 0, 1
-MMC_DEVERR_TIMEOUT, MMC_DEVERR_BADFREE, MMC_DEVERR_OOM = 0x1, 0x2, 0x4
+MMC_DEVERR_TIMEOUT, MMC_DEVERR_BADFREE, MMC_DEVERR_OOM, MMC_DEVERR_BADCMD = 0x1, 0x2, 0x4, 0x8
 MMC_SERVE_FREE, MMC_SERVE_LIVE, MMC_SERVE_DONE = 0, 1, 2
 
 u32, u64, i64, vp = ctypes.c_uint32, ctypes.c_uint64, ctypes.c_int64, ctypes.c_void_p
@@ -37,6 +37,7 @@ class MmcDeviceHandle(ctypes.Structure):
         ("hashingK", u32), ("hashingDistMP", u32), ("hashingDistWP", u32), ("hashingDistWPRel", u32),
         ("dataAlignment", u32), ("distribution", u32), ("oom_policy", u32), ("reference_quirks", u32),
         ("hierarchyThreshold", u32), ("minChunkSize", u32), ("paddedMinChunkSize", u32), ("maxOnPageMasks", u32),
+        ("zero", u32),
     ]
 
 
@@ -112,6 +113,7 @@ SIGNATURES = {
     "mmc_serve_queue": (ctypes.c_int, [vp, ctypes.POINTER(vp), ctypes.POINTER(vp), ctypes.POINTER(vp),
                                        ctypes.POINTER(vp)]),
     "mmc_serve_tick": (ctypes.c_int, [vp, ctypes.c_int]),
+    "mmc_serve_check_queue": (ctypes.c_int, [vp, u32, u32, u32]),
     "mmc_serve_pipeline": (ctypes.c_int, [vp, ctypes.c_int] + [ctypes.POINTER(vp)] * 6),
     "mmc_serve_launch": (ctypes.c_int, [vp, ctypes.c_int]),
     "mmc_serve_wait": (ctypes.c_int, [vp]),

@@ -5,7 +5,7 @@
  *   example03  device-side getAvailableSlots next to a live allocation
  *              (reference: examples/mallocMC_example03.cpp)
  * Built into libmallocmc_examples.so (linked against libmallocmc_gb300.so) and
- * driven by tests/test_cxx_api_gpu.py through the extern "C" wrappers below.
+ * driven by tests/test_cxx_api.py through the extern "C" wrappers below.
  *
  * Both reference examples construct a 1 GB heap with the default 2 GiB access
  * block; the reference divides by zero for that configuration

@@ -17,6 +17,8 @@
  */
 #include "mmc_internal.h"
 
+#include <cuda.h>
+
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
@@ -231,7 +233,48 @@ namespace
 {
     constexpr int kNoallocMaxDevices = 64;
     std::mutex g_noalloc_mutex;
-    SlotPartial* g_noalloc_addr[kNoallocMaxDevices] = {};
+    /* the array's device address per device ordinal, with the id of the
+     * context it was looked up in: after a cudaDeviceReset, or for a caller
+     * whose current context on that ordinal is another one, the ids differ
+     * and the address is looked up again */
+    struct NoallocAddr
+    {
+        unsigned long long ctx_id;
+        SlotPartial* addr;
+    };
+    NoallocAddr g_noalloc_addr[kNoallocMaxDevices] = {};
+
+    /* Unique id of the calling thread's current CUDA context (cuCtxGetId,
+     * reached through the runtime's driver entry points so the library does
+     * not link libcuda); 0 when there is none yet or the driver lacks it. */
+    unsigned long long current_context_id()
+    {
+        using GetCurrent = CUresult (*)(CUcontext*);
+        using GetId = CUresult (*)(CUcontext, unsigned long long*);
+        static GetCurrent get_current = nullptr;
+        static GetId get_id = nullptr;
+        static bool looked_up = false;
+        if(!looked_up)
+        {
+            looked_up = true;
+            void* f = nullptr;
+            cudaDriverEntryPointQueryResult q;
+            if(cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess
+               && q == cudaDriverEntryPointSuccess)
+                get_current = reinterpret_cast<GetCurrent>(f);
+            f = nullptr;
+            if(cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess
+               && q == cudaDriverEntryPointSuccess)
+                get_id = reinterpret_cast<GetId>(f);
+            cudaGetLastError();
+        }
+        CUcontext ctx = nullptr;
+        unsigned long long id = 0ull;
+        if(get_current == nullptr || get_id == nullptr || get_current(&ctx) != CUDA_SUCCESS || ctx == nullptr
+           || get_id(ctx, &id) != CUDA_SUCCESS)
+            return 0ull;
+        return id;
+    }
 } // namespace
 
 /* ------------------------------------------------------------- host logic */
@@ -331,6 +374,7 @@ namespace
         d.minChunkSize = (c.pagesize - 128u) / 1024u;
         d.paddedMinChunkSize = mmc::dev::apply_padding(c.dataAlignment, d.minChunkSize);
         d.maxOnPageMasks = g.maxOnPageMasks;
+        d.zero = 0u;
     }
 
     /* Shrink::alignPool (Shrink.hpp:109-130), including its size arithmetic. */
@@ -625,17 +669,21 @@ mmc_status mmc_available_slots_noalloc(const mmc_device_handle* handle, size_t s
                                      + std::to_string(MMC_NOALLOC_SCAN_BLOCKS_MAX) + " partials");
     SlotPartial* partials = nullptr;
     {
-        /* set-up, once per device, with that device current */
+        /* set-up, once per device and context, with that device current */
         std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-        if(g_noalloc_addr[dev] == nullptr)
+        NoallocAddr& a = g_noalloc_addr[dev];
+        const unsigned long long ctx = current_context_id();
+        if(a.addr == nullptr || ctx == 0ull || a.ctx_id != ctx)
         {
             void* p = nullptr;
             st = cuda_check(cudaGetSymbolAddress(&p, g_noalloc_partials), "cudaGetSymbolAddress");
             if(st != MMC_OK)
                 return st;
-            g_noalloc_addr[dev] = static_cast<SlotPartial*>(p);
+            /* the lookup makes the device's context current if it was not yet */
+            a.ctx_id = ctx != 0ull ? ctx : current_context_id();
+            a.addr = static_cast<SlotPartial*>(p);
         }
-        partials = g_noalloc_addr[dev];
+        partials = a.addr;
     }
     const uint32_t slot = mmc::dev::apply_padding(handle->dataAlignment, static_cast<uint32_t>(slot_size));
     const bool multi = slot >= handle->pagesize;

@@ -30,6 +30,7 @@
 
 #include <cstring>
 #include <new>
+#include <string>
 #include <vector>
 
 using namespace mmc::host;
@@ -99,14 +100,29 @@ struct mmc_server
 };
 
 /* Apply admissions (cmd.kind 1) and releases (cmd.kind 2), read from the
- * host's queue; each changed slot is also written to the host's table. */
+ * host's queue; each changed slot is also written to the host's table. The
+ * queue lives in host-written memory, so nothing in it is trusted: a length
+ * beyond the queue's capacity is cut to it, and a command naming a slot
+ * beyond the table or an unknown kind is skipped; either sets
+ * MMC_DEVERR_BADCMD in the heap's error word. */
 __global__ void mmc_serve_apply(mmc_serve_slot* slots, mmc_serve_slot* mirror, const mmc_serve_cmd* q,
-                                const uint32_t* qlen)
+                                const uint32_t* qlen, uint32_t queue_cap, uint32_t nslots, uint32_t* error_flags)
 {
-    const uint32_t n = *qlen;
+    uint32_t n = *qlen;
+    if(n > queue_cap)
+    {
+        if(blockIdx.x == 0u && threadIdx.x == 0u)
+            atomicOr(error_flags, MMC_DEVERR_BADCMD);
+        n = queue_cap;
+    }
     for(uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
     {
         const mmc_serve_cmd c = q[i];
+        if(c.slot >= nslots || (c.kind != 1u && c.kind != 2u))
+        {
+            atomicOr(error_flags, MMC_DEVERR_BADCMD);
+            continue;
+        }
         mmc_serve_slot& s = slots[c.slot];
         if(c.kind == 1u)
         {
@@ -303,7 +319,8 @@ namespace
     mmc_status enqueue_tick(mmc_server* s, bool batched)
     {
         cudaStream_t st = s->stream;
-        mmc_serve_apply<<<8, 128, 0, st>>>(s->d_slots, s->m_slots, s->m_queue, s->m_queue_len);
+        mmc_serve_apply<<<8, 128, 0, st>>>(s->d_slots, s->m_slots, s->m_queue, s->m_queue_len, s->queue_cap, s->slots,
+                                           &s->handle.state->error_flags);
         if(batched)
         {
             const uint32_t blocks = (s->slots + 7u) / 8u;
@@ -321,7 +338,8 @@ namespace
     {
         cudaStream_t st = s->stream;
         mmc_server::Pipe& p = s->pipe[b];
-        mmc_serve_apply<<<8, 128, 0, st>>>(s->d_slots, s->m_slots, p.m_queue, p.m_queue_len);
+        mmc_serve_apply<<<8, 128, 0, st>>>(s->d_slots, s->m_slots, p.m_queue, p.m_queue_len, s->queue_cap, s->slots,
+                                           &s->handle.state->error_flags);
         const uint32_t blocks = (s->slots + 7u) / 8u;
         mmc_serve_tick_kernel<<<blocks, 256, 0, st>>>(s->handle, s->d_slots, s->m_slots, s->d_chunks, s->slots,
                                                      s->max_chunks, s->step, p.d_done, p.d_counts);
@@ -485,10 +503,34 @@ mmc_status mmc_serve_pipeline(mmc_server* s, int buffer, mmc_serve_cmd** queue, 
     return MMC_OK;
 }
 
+mmc_status mmc_serve_check_queue(const mmc_serve_cmd* queue, uint32_t queue_len, uint32_t queue_cap, uint32_t slots)
+{
+    if(queue_len > queue_cap)
+        return fail(MMC_ERR_ARG, "queue length " + std::to_string(queue_len) + " exceeds the queue's capacity of "
+                                     + std::to_string(queue_cap) + " commands");
+    if(queue_len != 0u && queue == nullptr)
+        return fail(MMC_ERR_ARG, "queue is null");
+    for(uint32_t i = 0; i < queue_len; ++i)
+    {
+        if(queue[i].kind != 1u && queue[i].kind != 2u)
+            return fail(MMC_ERR_ARG, "command " + std::to_string(i) + " has unknown kind "
+                                         + std::to_string(queue[i].kind));
+        if(queue[i].slot >= slots)
+            return fail(MMC_ERR_ARG, "command " + std::to_string(i) + " names slot " + std::to_string(queue[i].slot)
+                                         + " of a table of " + std::to_string(slots));
+    }
+    return MMC_OK;
+}
+
 mmc_status mmc_serve_launch(mmc_server* s, int buffer)
 {
     if(s == nullptr || buffer < 0 || buffer > 1)
         return fail(MMC_ERR_ARG, "server is null or buffer not 0 or 1");
+    /* the tick on this buffer reads the queue the host has just written: check it first */
+    mmc_status q = mmc_serve_check_queue(s->pipe[buffer].h_queue, *s->pipe[buffer].h_queue_len, s->queue_cap,
+                                         s->slots);
+    if(q != MMC_OK)
+        return q;
     mmc_status st = cuda_check(cudaGraphLaunch(s->pipe[buffer].exec, s->stream), "pipelined tick launch");
     if(st == MMC_OK)
         st = cuda_check(cudaEventRecord(s->pipe[buffer].finished, s->stream), "record tick event");
@@ -529,7 +571,9 @@ mmc_status mmc_serve_tick(mmc_server* s, int batched)
 {
     if(s == nullptr)
         return fail(MMC_ERR_ARG, "server is null");
-    mmc_status st = MMC_OK;
+    mmc_status st = mmc_serve_check_queue(s->h_queue, *s->h_queue_len, s->queue_cap, s->slots);
+    if(st != MMC_OK)
+        return st;
     if(batched)
         st = cuda_check(cudaGraphLaunch(s->exec, s->stream), "tick graph launch");
     else
@@ -544,7 +588,8 @@ mmc_status mmc_serve_tick(mmc_server* s, int batched)
             live[w] = s->h_slots[w].state == MMC_SERVE_LIVE;
         for(uint32_t i = 0; i < *s->h_queue_len; ++i)
             live[s->h_queue[i].slot] = s->h_queue[i].kind == 1u;
-        mmc_serve_apply<<<8, 128, 0, stream>>>(s->d_slots, s->m_slots, s->m_queue, s->m_queue_len);
+        mmc_serve_apply<<<8, 128, 0, stream>>>(s->d_slots, s->m_slots, s->m_queue, s->m_queue_len, s->queue_cap,
+                                               s->slots, &s->handle.state->error_flags);
         for(uint32_t w = 0; w < s->slots; ++w)
             if(live[w])
                 mmc_serve_one_kernel<<<1, 32, 0, stream>>>(s->handle, s->d_slots, s->m_slots, s->d_chunks, w,

@@ -1,7 +1,7 @@
 """Generate the golden fixtures in tests/golden/ from the reference itself.
 
 Runs the UNMODIFIED reference headers (alpaka CPU-serial backend, built by
-`make -C oracle ref` into oracle/_ref/ref_harness) on seeded op programs and
+`make -C oracle ref REF=<reference tree>` into oracle/_ref/ref_harness) on seeded op programs and
 stores the programs together with the reference's outputs: pool offsets of
 every malloc, getAvailableSlots results (host and accelerator paths) and a
 metadata snapshot (PTEs, region counters, on-page masks, header words).

@@ -80,3 +80,41 @@ def test_cut_short_run_drains_before_the_next():
         srv.close()
         assert_all_free(alloc.snapshot(), pagesize=65536)
         assert alloc.error_flags() == 0
+
+
+def test_tick_refuses_a_bad_queue():
+    """A tick whose host-written queue is out of range (length beyond the
+    queue's capacity, a slot beyond the table, an unknown kind) is refused
+    with MMC_ERR_ARG before anything is launched, in the synchronous and the
+    pipelined form; a valid queue then ticks normally."""
+    from mallocmc_gb300 import _lib as L
+    from mallocmc_gb300.serve import Server
+
+    with _server_heap() as alloc:
+        srv = Server(alloc, slots=8, max_chunks=16, step=64, queue_cap=4)
+        lib = L.lib()
+        for batched in (1, 0):
+            srv.queue_len[0] = 5
+            assert lib.mmc_serve_tick(srv._s, batched) == L.MMC_ERR_ARG
+            srv.queue_len[0] = 1
+            srv.queue[0] = (1, 8, 0, 100, 1)
+            assert lib.mmc_serve_tick(srv._s, batched) == L.MMC_ERR_ARG
+            srv.queue[0] = (3, 0, 0, 100, 1)
+            assert lib.mmc_serve_tick(srv._s, batched) == L.MMC_ERR_ARG
+        pq = srv._pipe[0]["q"]
+        pql = srv._pipe[0]["qlen"]
+        pql[0] = 1
+        pq["kind"][0], pq["slot"][0] = 1, 9
+        assert lib.mmc_serve_launch(srv._s, 0) == L.MMC_ERR_ARG
+        pql[0] = 0
+        srv.queue[0] = (1, 2, 0, 100, 1)
+        assert lib.mmc_serve_tick(srv._s, 1) == L.MMC_OK
+        assert int(srv.slots["state"][2]) in (L.MMC_SERVE_LIVE, L.MMC_SERVE_DONE)
+        srv.queue_len[0] = 0
+        while int(srv.slots["state"][2]) != L.MMC_SERVE_DONE:
+            assert lib.mmc_serve_tick(srv._s, 1) == L.MMC_OK
+        srv.queue_len[0] = 1
+        srv.queue[0] = (2, 2, 0, 0, 0)
+        assert lib.mmc_serve_tick(srv._s, 1) == L.MMC_OK
+        srv.close()
+        assert alloc.error_flags() == 0

@@ -148,3 +148,31 @@ def test_pipelined_ticks_need_room_to_release_every_slot():
     srv = ModelServer(1000, slots=64, queue_cap=32)
     with pytest.raises(ValueError):
         srv.run(arrivals, lengths, seeds, batched=True, realtime=False, pipelined=True)
+
+
+def test_queue_check_refuses_out_of_range_commands():
+    """mmc_serve_check_queue, the host-side check every tick launch runs first:
+    a queue length beyond the queue's capacity, a slot beyond the table or an
+    unknown command kind is MMC_ERR_ARG; a valid queue is MMC_OK. No GPU."""
+    import ctypes
+
+    from mallocmc_gb300 import _lib as L
+    from mallocmc_gb300.serve import CMD_DTYPE
+
+    lib = L.lib()
+    q = np.zeros(4, dtype=CMD_DTYPE)
+    q["kind"] = [1, 2, 1, 1]
+    q["slot"] = [0, 7, 3, 5]
+    ptr = q.ctypes.data_as(ctypes.c_void_p)
+    assert lib.mmc_serve_check_queue(ptr, 4, 4, 8) == L.MMC_OK
+    assert lib.mmc_serve_check_queue(ptr, 0, 4, 8) == L.MMC_OK
+    assert lib.mmc_serve_check_queue(ptr, 5, 4, 8) == L.MMC_ERR_ARG
+    assert b"exceeds the queue's capacity" in lib.mmc_last_error()
+    q["slot"][1] = 8
+    assert lib.mmc_serve_check_queue(ptr, 4, 4, 8) == L.MMC_ERR_ARG
+    assert b"names slot 8" in lib.mmc_last_error()
+    q["slot"][1] = 7
+    q["kind"][2] = 3
+    assert lib.mmc_serve_check_queue(ptr, 4, 4, 8) == L.MMC_ERR_ARG
+    assert b"unknown kind" in lib.mmc_last_error()
+    assert lib.mmc_serve_check_queue(None, 1, 4, 8) == L.MMC_ERR_ARG

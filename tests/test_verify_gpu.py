@@ -315,3 +315,48 @@ def test_stress_full_size_steps_no_corruption():
         snap = alloc.snapshot()
         assert_all_free(snap)
         assert alloc.error_flags() == 0
+
+
+@pytest.mark.parametrize("quirks", [True, False])
+def test_page_based_hint_after_a_run_at_page_zero(quirks):
+    """Multi-page runs allocated one after another by real thread ids (the
+    lock-free search) fill a 64 MiB heap top-down, the last run ending at page
+    0; one run is freed and the next multi-page malloc tries again. The
+    reference stores page - 1 as the next search start, which wraps for a run
+    at page 0 (Scatter.hpp:800-804) and no later free can lower it again
+    (deallocPageBased's atomicMax, :885): the reference's mode reproduces the
+    failing malloc, the fixed mode (reference_quirks = 0) serves it from the
+    freed run. Every offset equals the oracle's serial run in the same mode."""
+    from mallocmc_gb300.workloads import alloc_offsets, free_offsets, program_arrays
+
+    cfg = HeapConfig(4096, 8 << 20, 16, 2, False, reference_quirks=quirks)
+    heap = 64 << 20
+    size = 232 * 4096  # 16240 pages = 70 runs of 232
+    with gpu_allocator(cfg, heap) as alloc:
+        g = alloc.geometry()
+        runs = g.numpages // 232
+        assert runs * 232 == g.numpages
+        got = []
+        for i in range(runs):
+            ds, offs_t = alloc_offsets(alloc, 1, 1, np.array([size], dtype=np.uint32), i)
+            got.append((ds, offs_t, i))
+        offs = np.array([int(o.cpu().item()) for _, o, _ in got])
+        assert np.all(offs >= 0) and offs[-1] == 0
+        hint = alloc.snapshot()[3]["firstFreePageBased"]
+        assert hint == (0xFFFFFFFF if quirks else 0)
+        ds, offs_t, seed = got[9]
+        assert free_offsets(alloc, 1, 1, ds, offs_t, seed) == 0
+        _, again_t = alloc_offsets(alloc, 1, 1, np.array([size], dtype=np.uint32), 99)
+        again = int(again_t.cpu().item())
+        if quirks:
+            assert again == -1
+        else:
+            assert again == int(offs[9])
+        oh = OracleHeap(cfg, heap)
+        ops = [("m", size)] * runs + [("f", 9), ("m", size)]
+        kinds, args = program_arrays(ops)
+        want = oh.run_program(kinds.tobytes(), args)
+        oh.close()
+        assert want[:runs].tolist() == offs.tolist()
+        assert int(want[-1]) == again
+        assert alloc.error_flags() == 0

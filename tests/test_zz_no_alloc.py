@@ -1,9 +1,10 @@
 """The free-slot count that allocates nothing (mmc_available_slots_noalloc).
 
-Callers that cannot call cudaMalloc (code running under a global-mode CUDA
-graph capture, or code that holds only a device handle inside a framework whose
-memory belongs to its own pool) count free slots through this entry point,
-whose scan scratch is a fixed 32 KiB device array instead of heap-owned memory.
+Callers that cannot call cudaMalloc (code inside a framework whose device
+memory belongs to its own pool allocator, a plugin handed only the device
+handle, a latency-bound host loop that cannot take cudaMalloc's device-wide
+synchronisation) count free slots through this entry point, whose scan
+scratch is a fixed 32 KiB device array instead of heap-owned memory.
 Its counts must equal those of the regular entry point (mmc_available_slots) on
 the same heap state, exactly, on two calls in a row. This file is named so
 pytest collects it last; it also passes alone in a fresh process.
