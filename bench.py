@@ -464,25 +464,31 @@ def fragmentation_column(torch, args, sms, atom_peak=None):
     tests/golden/frag_fill.json (ten minutes of CPU at this size). Run with the
     hash distances tuned for fill (hashingDistMP, WP and WPRel 0) and with the
     reference's defaults."""
-    from mallocmc_gb300 import AlignmentPolicies, Allocator, CreationPolicies, DistributionPolicies
+    from mallocmc_gb300.autotune import GB300_FRAG_TUNED, FragConfig, autotune_fragmentation, frag_allocator
     from mallocmc_gb300.fragmentation import run_fragmentation
 
     heap_bytes, ab, seed = 32 << 30, 256 << 20, 42
-    ref = None
-    if os.path.exists(FRAG_GOLDEN):
+
+    def golden(hb):
+        if not os.path.exists(FRAG_GOLDEN):
+            return None
         with open(FRAG_GOLDEN) as f:
             doc = json.load(f)
         for g in doc["geometries"]:
-            if g["heap_bytes"] == heap_bytes and g["accessblocksize"] == ab and doc["seed"] == seed:
-                ref = {"phase1_fill": g["phase1_fill"], "final_fill": g["final_fill"],
-                       "phase1_allocs": g["phase1_allocs"], "phase2_allocs": g["phase2_allocs"],
-                       "source": "oracle (serial reference algorithm), tests/golden/frag_fill.json"}
+            if g["heap_bytes"] == hb and g["accessblocksize"] == ab and doc["seed"] == seed:
+                return {"phase1_fill": g["phase1_fill"], "final_fill": g["final_fill"],
+                        "phase1_allocs": g["phase1_allocs"], "phase2_allocs": g["phase2_allocs"],
+                        "source": "oracle (serial reference algorithm), tests/golden/frag_fill.json"}
+        return None
+
+    ref = golden(heap_bytes)
+    tuned, trace = GB300_FRAG_TUNED, None
+    if args.autotune and golden(4 << 30) is not None:
+        tuned, trace = autotune_fragmentation(4 << 30, ab, golden(4 << 30), seed, sms * 2, 256)
     runs = {}
-    for label, (mp, wp, wprel) in (("tuned_hash", (0, 0, 0)), ("reference_hash", (17497, 1, 1))):
-        creation = CreationPolicies.Scatter(pagesize=4096, accessblocksize=ab, regionsize=16, wastefactor=2,
-                                            hashingDistMP=mp, hashingDistWP=wp, hashingDistWPRel=wprel)
-        alloc = Allocator(creation, DistributionPolicies.XMallocSIMD(4096), None, None, AlignmentPolicies.Shrink(16),
-                          size=heap_bytes)
+    for label, cfg in (("tuned_hash", tuned), ("reference_hash", FragConfig())):
+        mp, wp, wprel = cfg.hashingDistMP, cfg.hashingDistWP, cfg.hashingDistWPRel
+        alloc = frag_allocator(heap_bytes, ab, cfg)
         r = run_fragmentation(alloc, seed, sms * 2, 256, capacity=1 << 23)
         r["error_flags"] = alloc.error_flags()
         alloc.close()
@@ -497,10 +503,15 @@ def fragmentation_column(torch, args, sms, atom_peak=None):
             r["fill_vs_reference"] = {"phase1": r["phase1_fill"] - ref["phase1_fill"],
                                       "final": r["final_fill"] - ref["final_fill"]}
         runs[label] = r
-    return {"workload": "32 GiB heap, pagesize 4096, access block 256 MiB; 90% uniform [16, 2048] B, 10% "
-                        "log-uniform [8 KiB, 1 MiB]; fill to first NULL, free seeded half, refill to next NULL",
-            "unit": "ops/s (mallocs incl. the failing ones + frees) and fill = live requested bytes / heap bytes",
-            "reference": ref, **runs}
+    out = {"workload": "32 GiB heap, pagesize 4096, access block 256 MiB; 90% uniform [16, 2048] B, 10% "
+                       "log-uniform [8 KiB, 1 MiB]; fill to first NULL, free seeded half, refill to next NULL",
+           "unit": "ops/s (mallocs incl. the failing ones + frees) and fill = live requested bytes / heap bytes",
+           "tuned_hash_source": ("autotune_fragmentation in this run (4 GiB heap)" if trace is not None else
+                                 "mallocmc_gb300.autotune.GB300_FRAG_TUNED (autotune_fragmentation's pick on GB300)"),
+           "reference": ref, **runs}
+    if trace is not None:
+        out["autotune_trace"] = trace
+    return out
 
 
 def host_cores() -> int:

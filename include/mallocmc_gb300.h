@@ -128,9 +128,6 @@ typedef struct mmc_device_handle
     uint32_t minChunkSize;       /* (pagesize - 128) / 1024 */
     uint32_t paddedMinChunkSize; /* minChunkSize after alignment padding */
     uint32_t maxOnPageMasks;     /* min(32, ceil(pagesize / (32 * minChunkSize + 4))) */
-    uint32_t zero;               /* always 0: a value the compiler cannot know, which
-                                    mmc::dev::discard_dead_block folds into the freed
-                                    pointer to make the free depend on its reads */
 } mmc_device_handle;
 
 typedef struct mmc_heap mmc_heap;

@@ -37,7 +37,6 @@ class MmcDeviceHandle(ctypes.Structure):
         ("hashingK", u32), ("hashingDistMP", u32), ("hashingDistWP", u32), ("hashingDistWPRel", u32),
         ("dataAlignment", u32), ("distribution", u32), ("oom_policy", u32), ("reference_quirks", u32),
         ("hierarchyThreshold", u32), ("minChunkSize", u32), ("paddedMinChunkSize", u32), ("maxOnPageMasks", u32),
-        ("zero", u32),
     ]
 
 
@@ -126,6 +125,8 @@ SIGNATURES = {
 }
 
 _lib = None
+_stats_lib = None
+STATS_LIB_PATH = os.path.join(PKG, "libmallocmc_gb300_stats.so")
 
 
 class MallocMCError(RuntimeError):
@@ -148,6 +149,22 @@ def lib() -> ctypes.CDLL:
             fn.argtypes = args
         _lib = L
     return _lib
+
+
+def stats_lib() -> ctypes.CDLL:
+    """The same C ABI built with the device event counters (MMC_DEVICE_STATS):
+    mmc_heap_stats reports the MMC_STAT_* counts of heaps created through it."""
+    global _stats_lib
+    if _stats_lib is None:
+        if not os.path.exists(STATS_LIB_PATH):
+            raise RuntimeError(f"{STATS_LIB_PATH} is not built: run `python -m mallocmc_gb300.build`")
+        L = ctypes.CDLL(STATS_LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _stats_lib = L
+    return _stats_lib
 
 
 def check(status: int, what: str = ""):

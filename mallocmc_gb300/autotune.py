@@ -167,3 +167,83 @@ def autotune(jobs, heap_bytes: int, device: int = 0, passes: int = 2, repeats: i
         best = TuneConfig()
     trace = [{"config": asdict(c), "ms": ms} for c, ms in cache.items()]
     return best, best_ms, trace
+
+
+# ---------------------------------------------------------------- fragmentation
+#
+# The fragmentation workload (fill to the first NULL, free a seeded half,
+# refill to the next NULL) is judged by its fill at out-of-memory, which must
+# reach the reference's serial run on the same seed. What moves the fill most
+# is where the chunk pages of each size class land. The reference's hash
+# starts a request's page search at (size * hashingK + hashingDistMP * smid +
+# (hashingDistWP + hashingDistWPRel * reloff) * warpid) mod pagesperblock
+# (Scatter.hpp:531-551): on a CPU backend smid = warpid = 0, so every request
+# of one size starts at one page and chunk pages stay clustered; on 152 SMs x
+# 64 warps the default distances spread one size's chunk pages over the whole
+# access block, which breaks up the runs of free pages the multi-page requests
+# need, and the first NULL (a large request finding no run) comes sooner.
+# The candidates are (hashingDistMP, hashingDistWP, hashingDistWPRel).
+FRAG_HASHES = ((17497, 1, 1), (1, 0, 0), (0, 0, 0), (0, 1, 0), (17497, 0, 0), (101, 1, 0))
+
+
+@dataclass(frozen=True)
+class FragConfig:
+    hashingDistMP: int = 17497
+    hashingDistWP: int = 1
+    hashingDistWPRel: int = 1
+
+
+# The hash distances autotune_fragmentation picks for the bench's fragmentation
+# workload (4 KiB pages, 256 MiB access blocks, seed 42) on a GB300: the
+# largest fill margin over the reference's serial run in both phases.
+GB300_FRAG_TUNED = FragConfig(0, 0, 0)
+
+
+def frag_allocator(heap_bytes: int, accessblock: int, cfg: FragConfig, device: int = 0):
+    from .allocator import Allocator
+    from .policies import AlignmentPolicies, CreationPolicies, DistributionPolicies
+
+    creation = CreationPolicies.Scatter(pagesize=4096, accessblocksize=accessblock, regionsize=16, wastefactor=2,
+                                        hashingDistMP=cfg.hashingDistMP, hashingDistWP=cfg.hashingDistWP,
+                                        hashingDistWPRel=cfg.hashingDistWPRel)
+    return Allocator(creation, DistributionPolicies.XMallocSIMD(4096), None, None, AlignmentPolicies.Shrink(16),
+                     size=heap_bytes, device=device)
+
+
+def autotune_fragmentation(heap_bytes: int, accessblock: int, reference: dict, seed: int, blocks: int,
+                           threads_per_block: int = 256, candidates=FRAG_HASHES, repeats: int = 2, log=None):
+    """Run the fragmentation workload `repeats` times per candidate hash (each
+    on a fresh heap) and score it by its worst fill margin over the reference
+    (reference = {"phase1_fill", "final_fill"} of the serial run on the same
+    seed and geometry): the smaller of phase-1 and final margin over the
+    repeats. A run with a tag error is rejected. The largest margin wins, ties
+    within 1e-4 going to the faster. Returns (best, trace)."""
+    from .fragmentation import run_fragmentation
+
+    trace = []
+    for mp, wp, wprel in candidates:
+        cfg = FragConfig(mp, wp, wprel)
+        margins, rates, ok = [], [], True
+        for _ in range(repeats):
+            alloc = frag_allocator(heap_bytes, accessblock, cfg)
+            try:
+                r = run_fragmentation(alloc, seed, blocks, threads_per_block)
+                bad = r["tag_errors"] != 0 or r["list_overflow"] or alloc.error_flags() != 0
+            finally:
+                alloc.close()
+            if bad:
+                ok = False
+                break
+            margins.append(min(r["phase1_fill"] - reference["phase1_fill"], r["final_fill"] - reference["final_fill"]))
+            rates.append(r["ops_per_second"])
+        row = {"config": asdict(cfg), "ok": ok, "margin": min(margins) if ok else None,
+               "ops_per_second": statistics.median(rates) if ok else None}
+        trace.append(row)
+        if log:
+            log(row)
+    good = [t for t in trace if t["ok"]]
+    if not good:
+        return FragConfig(), trace
+    top = max(t["margin"] for t in good)
+    best = max((t for t in good if t["margin"] >= top - 1e-4), key=lambda t: t["ops_per_second"])
+    return FragConfig(**best["config"]), trace

@@ -4,6 +4,8 @@ Each translation unit under csrc/ is compiled in parallel with
 `nvcc -gencode arch=compute_103a,code=sm_103a -lineinfo -O3`, then linked into
 one shared library next to this file. No torch extension machinery: the
 library exports a plain C ABI (include/mallocmc_gb300.h) loaded with ctypes.
+The same sources are also built with the device event counters compiled in
+(-DMMC_DEVICE_STATS) into libmallocmc_gb300_stats.so, for tests and diagnosis.
 """
 from __future__ import annotations
 
@@ -20,6 +22,9 @@ INCLUDE = os.path.join(ROOT, "include")
 BUILD_DIR = os.path.join(PKG, "_build")
 LIB_NAME = "libmallocmc_gb300.so"
 LIB_PATH = os.path.join(PKG, LIB_NAME)
+# the same library with the device event counters (MMC_DEVICE_STATS) compiled in
+STATS_LIB_PATH = os.path.join(PKG, "libmallocmc_gb300_stats.so")
+STATS_BUILD_DIR = os.path.join(BUILD_DIR, "stats")
 EXAMPLES_PATH = os.path.join(PKG, "libmallocmc_examples.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["heap_capi.cu", "workloads.cu", "batch.cu", "serve.cu"]
@@ -79,6 +84,14 @@ def build(verbose: bool = False, ptxas_verbose: bool = False) -> str:
         if _stale(o, [s] + hdrs):
             cmd = [nvcc()] + _flags() + (["-Xptxas", "-v"] if ptxas_verbose else []) + ["-c", s, "-o", o]
             jobs.append(cmd)
+    os.makedirs(STATS_BUILD_DIR, exist_ok=True)
+    stats_objs = []
+    for src in SOURCES:
+        s = os.path.join(CSRC, src)
+        o = os.path.join(STATS_BUILD_DIR, src.replace(".cu", ".o"))
+        stats_objs.append(o)
+        if _stale(o, [s] + hdrs):
+            jobs.append([nvcc()] + _flags() + ["-DMMC_DEVICE_STATS", "-c", s, "-o", o])
 
     def run(cmd):
         r = subprocess.run(cmd, capture_output=True, text=True)
@@ -92,6 +105,11 @@ def build(verbose: bool = False, ptxas_verbose: bool = False) -> str:
                 raise RuntimeError(f"nvcc failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
     if _stale(LIB_PATH, objs):
         cmd = [nvcc()] + ARCH + ["-shared", "-cudart", "static", "-o", LIB_PATH] + objs
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    if _stale(STATS_LIB_PATH, stats_objs):
+        cmd = [nvcc()] + ARCH + ["-shared", "-cudart", "static", "-o", STATS_LIB_PATH] + stats_objs
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")

@@ -403,6 +403,7 @@ mmc_status mmc_batch_create(mmc_heap* heap, const mmc_job* jobs, uint32_t njobs,
 
 mmc_status mmc_batch_run(mmc_batch* b, void* stream)
 {
+    mmc::host::NvtxRange nvtx_range("mmc_batch_run");
     if(b == nullptr)
         return fail(MMC_ERR_ARG, "batch is null");
     cudaStream_t s = as_stream(stream);
@@ -414,6 +415,7 @@ mmc_status mmc_batch_run(mmc_batch* b, void* stream)
 
 mmc_status mmc_batch_run_plain(mmc_batch* b, void* stream)
 {
+    mmc::host::NvtxRange nvtx_range("mmc_batch_run_plain");
     if(b == nullptr)
         return fail(MMC_ERR_ARG, "batch is null");
     cudaStream_t s = as_stream(stream);

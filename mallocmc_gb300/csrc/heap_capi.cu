@@ -374,7 +374,6 @@ namespace
         d.minChunkSize = (c.pagesize - 128u) / 1024u;
         d.paddedMinChunkSize = mmc::dev::apply_padding(c.dataAlignment, d.minChunkSize);
         d.maxOnPageMasks = g.maxOnPageMasks;
-        d.zero = 0u;
     }
 
     /* Shrink::alignPool (Shrink.hpp:109-130), including its size arithmetic. */
@@ -543,6 +542,7 @@ mmc_status mmc_heap_create(const mmc_config* cfg, size_t bytes, int device, void
 mmc_status mmc_heap_create_on_pool(const mmc_config* cfg, void* pool, size_t bytes, int device, void* stream,
                                    mmc_heap** out)
 {
+    mmc::host::NvtxRange nvtx_range("mmc_heap_create");
     return create_common(cfg, pool, bytes, false, device, stream, out);
 }
 
@@ -645,6 +645,7 @@ mmc_status mmc_heap_info(const mmc_heap* h, char* buf, size_t len)
 
 mmc_status mmc_available_slots_async(mmc_heap* h, size_t slot_size, void* stream, unsigned* out_dev)
 {
+    mmc::host::NvtxRange nvtx_range("mmc_available_slots");
     if(h == nullptr || out_dev == nullptr)
         return fail(MMC_ERR_ARG, "null argument");
     const uint32_t slot = mmc::dev::apply_padding(h->cfg.dataAlignment, static_cast<uint32_t>(slot_size));

@@ -5,6 +5,7 @@
 #include "mallocMC/scatter_device.cuh"
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <string>
 
@@ -28,5 +29,17 @@ namespace mmc
 
         /* Device-side word that receives the result of mmc_available_slots. */
         unsigned* slots_result_word(mmc_heap* heap);
+
+        /* An NVTX range over a host entry point's work (heap set-up, slot
+         * counts, launches of the batched and serving kernels), so Nsight
+         * tools show each phase by name; without a tool attached it costs a
+         * call into an empty stub. */
+        struct NvtxRange
+        {
+            explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+            ~NvtxRange() { nvtxRangePop(); }
+            NvtxRange(const NvtxRange&) = delete;
+            NvtxRange& operator=(const NvtxRange&) = delete;
+        };
     } // namespace host
 } // namespace mmc

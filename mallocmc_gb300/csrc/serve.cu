@@ -524,6 +524,7 @@ mmc_status mmc_serve_check_queue(const mmc_serve_cmd* queue, uint32_t queue_len,
 
 mmc_status mmc_serve_launch(mmc_server* s, int buffer)
 {
+    mmc::host::NvtxRange nvtx_range("mmc_serve_launch");
     if(s == nullptr || buffer < 0 || buffer > 1)
         return fail(MMC_ERR_ARG, "server is null or buffer not 0 or 1");
     /* the tick on this buffer reads the queue the host has just written: check it first */
@@ -569,6 +570,7 @@ mmc_status mmc_serve_queue(mmc_server* s, mmc_serve_cmd** queue, uint32_t** queu
 
 mmc_status mmc_serve_tick(mmc_server* s, int batched)
 {
+    mmc::host::NvtxRange nvtx_range("mmc_serve_tick");
     if(s == nullptr)
         return fail(MMC_ERR_ARG, "server is null");
     mmc_status st = mmc_serve_check_queue(s->h_queue, *s->h_queue_len, s->queue_cap, s->slots);

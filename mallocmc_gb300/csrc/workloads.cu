@@ -166,7 +166,7 @@ __global__ void __launch_bounds__(256, 4) mmc_stress_kernel(mmc_device_handle h,
             else
             {
                 /* the verified block is dead: its whole lines leave L2 unwritten */
-                dv::free<dv::GpuIds>(h, dv::discard_dead_block(h, ptr, bytes));
+                dv::free<dv::GpuIds>(h, dv::discard_dead_block(ptr, bytes));
                 ++pairs;
             }
             continue;
@@ -214,7 +214,7 @@ __global__ void __launch_bounds__(256, 4) mmc_stress_kernel(mmc_device_handle h,
 
 /* The same stress on CUDA's device heap (CreationPolicies::OldMalloc, OldMalloc.hpp:59-68). */
 __global__ void __launch_bounds__(256) mmc_stress_oldmalloc_kernel(mmc_stress_params p, const uint16_t* sizes,
-                                                                   unsigned long long* stats, uint32_t zero)
+                                                                   unsigned long long* stats)
 {
     const uint64_t nthreads = static_cast<uint64_t>(gridDim.x) * blockDim.x;
     const uint64_t t = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -233,7 +233,7 @@ __global__ void __launch_bounds__(256) mmc_stress_oldmalloc_kernel(mmc_stress_pa
                 ++nulls;
             else
             {
-                ::free(dv::discard_dead_block(ptr, bytes, zero)); /* as the GB300 heap's stress does */
+                ::free(dv::discard_dead_block(ptr, bytes)); /* as the GB300 heap's stress does */
                 ++pairs;
             }
             continue;
@@ -494,6 +494,7 @@ mmc_status mmc_run_program(mmc_heap* heap, const uint8_t* kinds, const uint64_t*
 mmc_status mmc_run_stress(mmc_heap* heap, const mmc_stress_params* p, const uint16_t* sizes,
                           unsigned long long* stats, void* stream)
 {
+    mmc::host::NvtxRange nvtx_range("mmc_run_stress");
     if(heap == nullptr || p == nullptr || stats == nullptr)
         return fail(MMC_ERR_ARG, "null argument");
     if(p->blocks == 0u || p->threads_per_block == 0u || p->threads_per_block > 256u || p->step == 0u
@@ -531,8 +532,7 @@ mmc_status mmc_run_stress_oldmalloc(const mmc_stress_params* p, const uint16_t* 
     if(p->blocks == 0u || p->threads_per_block == 0u || p->threads_per_block > 256u || p->step == 0u
        || p->hi < p->lo || (p->write_pattern == MMC_PATTERN_WARP && (p->threads_per_block % 32u) != 0u))
         return fail(MMC_ERR_ARG, "bad stress parameters");
-    /* zero: the run-time 0 discard_dead_block folds into each freed pointer */
-    mmc_stress_oldmalloc_kernel<<<p->blocks, p->threads_per_block, 0, as_stream(stream)>>>(*p, sizes, stats, 0u);
+    mmc_stress_oldmalloc_kernel<<<p->blocks, p->threads_per_block, 0, as_stream(stream)>>>(*p, sizes, stats);
     return cuda_check(cudaGetLastError(), "OldMalloc stress kernel");
 }
 
@@ -575,6 +575,7 @@ mmc_status mmc_run_free_offsets(mmc_heap* heap, uint32_t blocks, uint32_t tpb, c
 mmc_status mmc_run_fill(mmc_heap* heap, const mmc_frag_params* p, void** ptrs, uint32_t* sizes, uint64_t capacity,
                         unsigned long long* counters, void* stream)
 {
+    mmc::host::NvtxRange nvtx_range("mmc_run_fill");
     if(heap == nullptr || p == nullptr || ptrs == nullptr || sizes == nullptr || counters == nullptr)
         return fail(MMC_ERR_ARG, "null argument");
     if(p->blocks == 0u || p->threads_per_block == 0u || p->threads_per_block > 256u || p->small_lo < 8u
@@ -596,6 +597,7 @@ mmc_status mmc_run_fill(mmc_heap* heap, const mmc_frag_params* p, void** ptrs, u
 mmc_status mmc_run_free_list(mmc_heap* heap, void** ptrs, uint32_t* sizes, const uint32_t* idx, uint64_t n,
                              unsigned long long* counters, void* stream)
 {
+    mmc::host::NvtxRange nvtx_range("mmc_run_free_list");
     if(heap == nullptr || ptrs == nullptr || sizes == nullptr || idx == nullptr || counters == nullptr)
         return fail(MMC_ERR_ARG, "null argument");
     if(n == 0u)

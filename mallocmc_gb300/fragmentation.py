@@ -39,14 +39,33 @@ def algorithmic_atomics(sizes, freed, pagesize: int) -> int:
     return atomics
 
 
+def mean_request_bytes(small=(16, 2048), large=(8192, 1 << 20), large_permille=100) -> float:
+    """Expected size of one request: uniform small sizes, log-uniform large ones."""
+    import math
+
+    ms = (small[0] + small[1]) / 2.0
+    ml = (large[1] - large[0]) / math.log(large[1] / large[0])
+    return (1000 - large_permille) / 1000.0 * ms + large_permille / 1000.0 * ml
+
+
 def run_fragmentation(alloc: Allocator, seed: int, blocks: int, threads_per_block: int = 256,
                       capacity: int = 1 << 22, small=(16, 2048), large=(8192, 1 << 20), large_permille=100,
-                      stream=None, waves_per_call: int = 8, max_waves: int = 1 << 20, release: bool = False) -> dict:
-    """Phase 1 fills from request 0 in waves of blocks*threads_per_block
-    requests until a wave meets a NULL; a seeded half of the live blocks is
-    freed; phase 2 continues with the next unused request index until the next
-    NULL. Returns fill fractions, counts, timings and the tag-error count. With
-    release, every block still live is then freed (its tags checked first)."""
+                      stream=None, waves_per_call: int = 8, max_waves: int = 1 << 20, release: bool = False,
+                      wave_fraction: float | None = 0.5, min_wave: int = 32) -> dict:
+    """Phase 1 fills from request 0 in waves of concurrent requests until a
+    wave meets a NULL; a seeded half of the live blocks is freed; phase 2
+    continues with the next unused request index until the next NULL. Returns
+    fill fractions, counts, timings and the tag-error count. With release,
+    every block still live is then freed (its tags checked first).
+
+    Wave sizes: with wave_fraction (the default), each wave is admitted by
+    free memory, as the serving loop admits requests: it holds as many
+    requests as wave_fraction of the heap's free bytes is expected to take
+    (mean_request_bytes), at least min_wave and at most
+    blocks * threads_per_block, rounded up to whole warps. Waves are large
+    while the heap is empty and shrink as it fills, so the requests that meet
+    the first NULL go out a few at a time, as in a serial run. With
+    wave_fraction None every wave is blocks * threads_per_block requests."""
     import torch
 
     lib = L.lib()
@@ -59,25 +78,37 @@ def run_fragmentation(alloc: Allocator, seed: int, blocks: int, threads_per_bloc
     out = {"heap_bytes": heap_bytes}
 
     T = blocks * threads_per_block
+    per_request = mean_request_bytes(small, large, large_permille)
 
     def fill(first):
-        """Waves from request `first` until the stop flag; returns (seconds, waves)."""
+        """Waves from request `first` until the stop flag; returns (seconds,
+        waves, requests issued)."""
         ctr[4] = 0
         torch.cuda.synchronize(dev)
         t0 = time.perf_counter()
-        waves = 0
+        waves = issued = 0
         while waves < max_waves:
-            p = frag_params(blocks, threads_per_block, seed, first + waves * T, small, large, large_permille,
-                            waves_per_call)
+            if wave_fraction is None:
+                p = frag_params(blocks, threads_per_block, seed, first + issued, small, large, large_permille,
+                                waves_per_call)
+                n, waves = waves_per_call * T, waves + waves_per_call
+            else:
+                free = max(0, heap_bytes - int(ctr[1].item()))
+                n = min(T, max(min_wave, int(wave_fraction * free / per_request)))
+                tpb = threads_per_block if n >= threads_per_block else 32
+                nb = -(-n // tpb)
+                n = nb * tpb
+                p = frag_params(nb, tpb, seed, first + issued, small, large, large_permille, 1)
+                waves += 1
             L.check(lib.mmc_run_fill(alloc.handle_ptr, ctypes.byref(p), ptrs.data_ptr(), sizes.data_ptr(),
                                      capacity, ctr.data_ptr(), s), "fill")
-            waves += waves_per_call
+            issued += n
             if int(ctr[4].item()) != 0:
                 break
         torch.cuda.synchronize(dev)
-        return time.perf_counter() - t0, waves
+        return time.perf_counter() - t0, waves, issued
 
-    t1, w1 = fill(0)
+    t1, w1, issued1 = fill(0)
     c = ctr.cpu().numpy().view(np.uint64)
     n1, live1, req1 = int(c[0]), int(c[1]), int(c[2])
     out.update(phase1_allocs=n1, phase1_requests=req1, phase1_live_bytes=live1, phase1_fill=live1 / heap_bytes,
@@ -90,7 +121,7 @@ def run_fragmentation(alloc: Allocator, seed: int, blocks: int, threads_per_bloc
                                   ctr.data_ptr(), s), "free_list")
     torch.cuda.synchronize(dev)
     tf = time.perf_counter() - t0
-    t2, w2 = fill(w1 * T)
+    t2, w2, issued2 = fill(issued1)
     c = ctr.cpu().numpy().view(np.uint64)
     n_total, live2, req_total = int(c[0]), int(c[1]), int(c[2])
     L.check(lib.mmc_run_verify_list(alloc.handle_ptr, ptrs.data_ptr(), sizes.data_ptr(), min(n_total, capacity),
@@ -103,8 +134,10 @@ def run_fragmentation(alloc: Allocator, seed: int, blocks: int, threads_per_bloc
     out.update(freed=len(half), phase2_allocs=n_total - n1, final_live_bytes=live2, final_fill=live2 / heap_bytes,
                algorithmic_atomics=atomics, atomics_per_second=atomics / (t1 + tf + t2),
                tag_errors=int(c[3]), free_seconds=tf, phase2_seconds=t2,
-               ops_per_second=ops / (t1 + tf + t2), list_overflow=n_total > capacity, wave_requests=T,
-               waves=(w1, w2))
+               ops_per_second=ops / (t1 + tf + t2), list_overflow=n_total > capacity, max_wave_requests=T,
+               waves=(w1, w2), requests_issued=(issued1, issued2),
+               wave_sizing=("admitted by free memory: %g of the free bytes per wave, %d to %d requests"
+                            % (wave_fraction, min_wave, T)) if wave_fraction is not None else "fixed")
     if release:
         n = min(n_total, capacity)
         every = torch.arange(n, dtype=torch.int32, device=dev)

@@ -96,3 +96,36 @@ def test_batch_beyond_the_shared_job_table():
         assert np.array_equal(plain[:, 0].astype(np.int64), want)
         assert np.array_equal(plain, batched)
         assert alloc.error_flags() == 0
+
+
+def test_full_size_batched_workload():
+    """The bench's batched workload at its full size: 512 jobs (thread counts
+    log-uniform in [32, 65536], 3.9 M job threads), one 16 GiB heap on the
+    autotuned geometry. Every job's pair count equals the host's count of its
+    cycle draws, no allocation fails, no pattern breaks, the persistent graph
+    launch and the per-job launches give each job the same checksum, and the
+    heap is empty afterwards."""
+    from mallocmc_gb300 import AlignmentPolicies, Allocator, CreationPolicies, DistributionPolicies
+    from mallocmc_gb300.autotune import GB300_TUNED as cfg
+    from mallocmc_gb300.autotune import _accessblock
+    from mallocmc_gb300.batch import Batch, expected_pairs, make_jobs
+
+    heap = 16 << 30
+    jobs = make_jobs(512, seed=3)
+    want = expected_pairs(jobs)
+    creation = CreationPolicies.Scatter(pagesize=cfg.pagesize, regionsize=cfg.regionsize,
+                                        accessblocksize=_accessblock(heap, cfg.pagesize, cfg.accessblock_fraction),
+                                        hashingK=cfg.hashingK, hashingDistMP=cfg.hashingDistMP)
+    with Allocator(creation, DistributionPolicies.XMallocSIMD(cfg.pagesize), None, None,
+                   AlignmentPolicies.Shrink(16), size=heap) as alloc:
+        b = Batch(alloc, jobs, persistent_blocks=152 * cfg.blocks_per_sm, use_graph=True)
+        b.run_plain()
+        plain = b.stats()
+        b.run()
+        graph = b.stats()
+        b.close()
+        assert np.array_equal(plain[:, 0].astype(np.int64), want)
+        assert int(plain[:, 1].sum()) == 0 and int(plain[:, 2].sum()) == 0
+        assert np.array_equal(plain, graph)
+        assert_all_free(alloc.snapshot(), pagesize=cfg.pagesize)
+        assert alloc.error_flags() == 0

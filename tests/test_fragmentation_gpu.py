@@ -16,24 +16,45 @@ SEED = 42
 
 
 def _allocator(heap, ab, mp, wp, wprel):
-    from mallocmc_gb300 import AlignmentPolicies, Allocator, CreationPolicies, DistributionPolicies
+    from mallocmc_gb300.autotune import FragConfig, frag_allocator
 
-    creation = CreationPolicies.Scatter(pagesize=4096, accessblocksize=ab, hashingDistMP=mp, hashingDistWP=wp,
-                                        hashingDistWPRel=wprel)
-    return Allocator(creation, DistributionPolicies.XMallocSIMD(4096), None, None, AlignmentPolicies.Shrink(16),
-                     size=heap)
+    return frag_allocator(heap, ab, FragConfig(mp, wp, wprel))
 
 
-@pytest.mark.parametrize("heap,ab,blocks,tpb", [(1 << 30, 256 << 20, 152, 64), (1 << 30, 64 << 20, 304, 256)])
-def test_fill_reaches_the_oracle(heap, ab, blocks, tpb):
-    """Hash distances for fill (hashingDistMP 1, WP 0): starts of one size class
-    stay within a few hundred pages, so chunk pages stay clustered the way the
-    serial run's are; the oracle's serial fill does not depend on them."""
+def _golden(heap, ab):
+    import json
+    import os
+
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "frag_fill.json")
+    with open(path) as f:
+        doc = json.load(f)
+    assert doc["seed"] == SEED
+    for g in doc["geometries"]:
+        if g["heap_bytes"] == heap and g["accessblocksize"] == ab:
+            return g
+    return None
+
+
+@pytest.mark.parametrize("heap", [1 << 30, 4 << 30])
+def test_fill_reaches_the_reference(heap):
+    """The workload's criterion as stated: with the hash distances the bench
+    uses (the autotuner's pick, GB300_FRAG_TUNED) and the bench's wave shape
+    (SMs x 2 blocks of 256 threads), the fill at the first NULL and after the
+    free-half-refill must each be at least the reference's serial run's on the
+    same seed and geometry (the oracle's run, recorded from the reference
+    algorithm in tests/golden/frag_fill.json)."""
+    import torch
+
+    from mallocmc_gb300.autotune import GB300_FRAG_TUNED
     from mallocmc_gb300.fragmentation import run_fragmentation
 
-    want = OracleHeap(HeapConfig(4096, ab, 16, 2, False), heap).run_fragmentation(SEED)
-    with _allocator(heap, ab, 1, 0, 0) as alloc:
-        r = run_fragmentation(alloc, SEED, blocks, tpb, release=True)
+    ab = 256 << 20
+    want = _golden(heap, ab)
+    assert want is not None
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    t = GB300_FRAG_TUNED
+    with _allocator(heap, ab, t.hashingDistMP, t.hashingDistWP, t.hashingDistWPRel) as alloc:
+        r = run_fragmentation(alloc, SEED, sms * 2, 256, release=True)
         assert r["tag_errors"] == 0 and not r["list_overflow"]
         assert alloc.error_flags() == 0
         assert r["released_live_bytes"] == 0
@@ -41,8 +62,30 @@ def test_fill_reaches_the_oracle(heap, ab, blocks, tpb):
         ptes = alloc.snapshot()[0]
         # no page-based run is left claimed: a page is either unformatted or a formatted chunk page
         assert int(np.count_nonzero(ptes[:, 0] > 4096)) == 0
+    assert r["phase1_fill"] >= want["phase1_fill"], (r["phase1_fill"], want["phase1_fill"])
+    assert r["final_fill"] >= want["final_fill"], (r["final_fill"], want["final_fill"])
+
+
+def test_fill_matches_the_oracle_on_a_fresh_geometry():
+    """Same criterion on a geometry with no recorded fixture (64 MiB access
+    blocks), against the oracle run here, with narrower waves."""
+    import torch
+
+    from mallocmc_gb300.autotune import GB300_FRAG_TUNED
+    from mallocmc_gb300.fragmentation import run_fragmentation
+
+    heap, ab = 1 << 30, 64 << 20
+    oh = OracleHeap(HeapConfig(4096, ab, 16, 2, False), heap)
+    want = oh.run_fragmentation(SEED)
+    oh.close()
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    t = GB300_FRAG_TUNED
+    with _allocator(heap, ab, t.hashingDistMP, t.hashingDistWP, t.hashingDistWPRel) as alloc:
+        r = run_fragmentation(alloc, SEED, sms, 256, release=True)
+        assert r["tag_errors"] == 0 and r["released_live_bytes"] == 0
+        assert alloc.error_flags() == 0
+    assert r["phase1_fill"] >= want["phase1_live_bytes"] / heap
     assert r["final_fill"] >= want["final_live_bytes"] / heap
-    assert r["phase1_fill"] >= 0.97 * want["phase1_live_bytes"] / heap
 
 
 def test_default_hash_keeps_tags_and_frees_everything():

@@ -118,3 +118,30 @@ def test_tick_refuses_a_bad_queue():
         assert lib.mmc_serve_tick(srv._s, 1) == L.MMC_OK
         srv.close()
         assert alloc.error_flags() == 0
+
+
+def test_serving_on_a_16_gib_heap_at_a_realistic_rate():
+    """The serving configuration's shape on a 16 GiB heap of 64 KiB pages:
+    Poisson arrivals at 20 k requests/s (simulated clock), lognormal lengths
+    (median 1024, sigma 1, cap 32768), 4096 slots, pipelined graph ticks.
+    Every request completes with the checksum it has alone, each of a few
+    requests run alone matches, and the heap is empty afterwards."""
+    from mallocmc_gb300 import AlignmentPolicies, Allocator, CreationPolicies, DistributionPolicies
+    from mallocmc_gb300.serve import Server, expected_checksum, make_requests
+
+    heap = 16 << 30
+    creation = CreationPolicies.Scatter(pagesize=65536, accessblocksize=4 << 30, regionsize=16)
+    arrivals, lengths, seeds = make_requests(4000, rate=20000, seed=20000)
+    want = np.array([expected_checksum(int(s), int(n)) for s, n in zip(seeds, lengths)], dtype=np.uint64)
+    with Allocator(creation, DistributionPolicies.XMallocSIMD(65536), None, None, AlignmentPolicies.Shrink(16),
+                   size=heap) as alloc:
+        srv = Server(alloc, slots=4096, max_chunks=128, step=64, queue_cap=8192)
+        mix = srv.run(arrivals, lengths, seeds, batched=True, realtime=False, pipelined=True)
+        assert mix["completed"] == len(arrivals)
+        assert np.array_equal(mix["checksum"], want)
+        for i in (0, 123, 3999):
+            alone = srv.run(arrivals[i:i + 1], lengths[i:i + 1], seeds[i:i + 1], batched=True, realtime=False)
+            assert alone["checksum"][0] == want[i] == mix["checksum"][i]
+        srv.close()
+        assert_all_free(alloc.snapshot(), pagesize=65536)
+        assert alloc.error_flags() == 0
