@@ -168,6 +168,48 @@ namespace mmc
             atomicOr(&h.state->error_flags, bits);
         }
 
+        /* ------------------------------------------------ free-page bitmap
+         * h.freemap has one bit per page, set while the page's chunk size is
+         * 0; the concurrent multi-page search reads it instead of the chunk
+         * sizes, 32 pages per word (no counterpart in the reference, which
+         * scans the page table). The chunk size stays the authority: a run is
+         * owned only once markpages' CASes succeed, so a bit set on a used
+         * page costs the search a failed CAS, as a lost run does. What must
+         * not happen is a clear bit on a free page for longer than a free is
+         * in flight, or the search would skip free pages. So: every change of
+         * a chunk size to 0 (a free, a page reset, a markpages roll-back) sets
+         * the bit after its CAS; every change from 0 clears the bit either
+         * before its CAS, or after it while nothing can free the page yet
+         * (markpages' run before it is handed out; a reset-mode format while
+         * the caller holds a fill slot), and a fence then waits for the clear
+         * to be performed, so no clear can land after a later free's set. */
+        __device__ __forceinline__ void freemap_clear_acked(u32* fm, u32 page)
+        {
+            atomicAnd(&fm[page >> 5], ~(1u << (page & 31u)));
+            asm volatile("fence.acq_rel.gpu;" ::: "memory");
+        }
+
+        __device__ __forceinline__ void freemap_set(u32* fm, u32 page)
+        {
+            atomicOr(&fm[page >> 5], 1u << (page & 31u));
+        }
+
+        /* set (free) or clear the bits of pages [first, first + n), one atomic per word */
+        __device__ inline void freemap_range(u32* fm, u32 first, u32 n, bool free)
+        {
+            for(u32 p = first, end = first + n; p < end;)
+            {
+                const u32 b = p & 31u;
+                const u32 cnt = umin(32u - b, end - p);
+                const u32 mask = cnt == 32u ? 0xFFFFFFFFu : ((1u << cnt) - 1u) << b;
+                if(free)
+                    atomicOr(&fm[p >> 5], mask);
+                else
+                    atomicAnd(&fm[p >> 5], ~mask);
+                p += cnt;
+            }
+        }
+
         /* nextspot, Scatter.hpp:293-304 */
         __device__ __forceinline__ u32 nextspot(u32 bitfield, u32 spot, u32 spots)
         {
@@ -329,6 +371,8 @@ namespace mmc
             if(h.resetfreedpages && filllevel < h.pagesize)
             {
                 const u32 oldChunksize = atomicCAS(&h.chunksize[page], 0u, chunksize);
+                if(oldChunksize == 0u)
+                    freemap_clear_acked(h.freemap, page); /* our fill slot keeps the page from a reset */
                 if(oldChunksize == 0u || (oldChunksize >= lo && oldChunksize <= hi))
                     tryAllocMem = true;
                 if(oldChunksize != 0u && oldChunksize != chunksize)
@@ -357,7 +401,10 @@ namespace mmc
                                                       u32 minAllocation, u32 maxchunksize)
         {
             if(before == 0u)
+            {
+                freemap_clear_acked(h.freemap, page);
                 before = atomicCAS(&h.chunksize[page], 0u, minAllocation);
+            }
             u32 use = 0u;
             if(before == 0u)
                 use = minAllocation;
@@ -611,7 +658,10 @@ namespace mmc
                 {
                     u32 before = visited == 0u ? cs0 : ld_rlx(&h.chunksize[page]);
                     if(before == 0u)
+                    {
+                        freemap_clear_acked(h.freemap, page);
                         before = atomicCAS(&h.chunksize[page], 0u, minAllocation);
+                    }
                     use = before == 0u ? minAllocation : ((before >= bytes && before <= maxchunksize) ? before : 0u);
                     if(use > h.hierarchyThreshold)
                         got = claim_bits_on_page(h, page, use, k - served);
@@ -725,7 +775,8 @@ namespace mmc
                     /* no chunk is live under the lock: drop any segment hint a
                      * race left behind (a no-op for the reference's serial runs) */
                     atomicExch(&h.bitmask[page], 0u);
-                    atomicCAS(&h.chunksize[page], chunksize, 0u);
+                    if(atomicCAS(&h.chunksize[page], chunksize, 0u) == chunksize)
+                        freemap_set(h.freemap, page);
                     __threadfence();
                     atomicSub(&h.count[page], P);
                 }
@@ -766,9 +817,14 @@ namespace mmc
                 }
             }
             if(abord == 0xFFFFFFFFu)
+            {
+                freemap_range(h.freemap, startpage, pages, false);
+                asm volatile("fence.acq_rel.gpu;" ::: "memory");
                 return true;
+            }
             for(u32 trypage = startpage; trypage < abord; ++trypage)
-                atomicCAS(&h.chunksize[trypage], bytes, 0u);
+                if(atomicCAS(&h.chunksize[trypage], bytes, 0u) == bytes)
+                    freemap_set(h.freemap, trypage);
             return false;
         }
 
@@ -840,6 +896,7 @@ namespace mmc
         struct PageScan
         {
             u32* chunksize;
+            u32* freemap;
             mmc_heap_state* state;
             char* pages;
             u32 numpages;
@@ -850,7 +907,9 @@ namespace mmc
         /* markpages (Scatter.hpp:745-764) for concurrent callers: the CASes go
          * out 4 at a time (independent atomics in flight together, not one
          * round trip per page); on a failure every page this call set is put
-         * back with CAS(bytes -> 0), as the reference's roll-back does. With no
+         * back with CAS(bytes -> 0), as the reference's roll-back does, and
+         * gets its free-page bit back. A run that is marked has its bits
+         * cleared (and the clears performed) before it is handed out. With no
          * concurrent caller the outcome is the serial form's. */
         __device__ __forceinline__ bool markpages_batched(const PageScan& c, u32 startpage, u32 pages, u32 bytes,
                                                           u32& free_below)
@@ -869,88 +928,147 @@ namespace mmc
                 if(lost != 0u)
                 {
                     for(u32 trypage = startpage; trypage < base; ++trypage)
-                        atomicCAS(&c.chunksize[trypage], bytes, 0u);
+                        if(atomicCAS(&c.chunksize[trypage], bytes, 0u) == bytes)
+                            freemap_set(c.freemap, trypage);
 #pragma unroll
                     for(u32 k = 0; k < 4u; ++k)
-                        if(base + k < end && ((lost >> k) & 1u) == 0u)
-                            atomicCAS(&c.chunksize[base + k], bytes, 0u);
+                        if(base + k < end && ((lost >> k) & 1u) == 0u
+                           && atomicCAS(&c.chunksize[base + k], bytes, 0u) == bytes)
+                            freemap_set(c.freemap, base + k);
                     /* the pages from startpage up to the lowest lost one were free */
                     free_below = base + static_cast<u32>(__ffs(static_cast<int>(lost))) - 1u - startpage;
                     return false;
                 }
             }
+            freemap_range(c.freemap, startpage, pages, false);
+            asm volatile("fence.acq_rel.gpu;" ::: "memory");
             return true;
         }
 
+        constexpr u32 kNoRun = 0xFFFFFFFFu;
+
+        /* Bits b_hi down to b_lo of free-page word w (value x), continuing a
+         * downward count of consecutive free pages: returns the first page of
+         * a run of n free pages once the count reaches n, else kNoRun. A used
+         * page resets the count and marks the search as having passed one. */
+        __device__ __forceinline__ u32 scan_freemap_word(u32 x, u32 w, u32 b_hi, u32 b_lo, u32 n, u32& freecount,
+                                                         bool& left_free)
+        {
+            const u32 span = b_hi - b_lo + 1u;
+            const u32 mask = span == 32u ? 0xFFFFFFFFu : ((1u << span) - 1u) << b_lo;
+            const u32 xm = x & mask;
+            if(xm == mask)
+            {
+                if(freecount + span >= n)
+                    return 32u * w + b_hi - (n - freecount - 1u);
+                freecount += span;
+                return kNoRun;
+            }
+            if(xm == 0u)
+            {
+                freecount = 0u;
+                left_free = true;
+                return kNoRun;
+            }
+            for(u32 b = b_hi + 1u; b-- > b_lo;)
+            {
+                if((xm >> b) & 1u)
+                {
+                    if(++freecount == n)
+                        return 32u * w + b;
+                }
+                else
+                {
+                    freecount = 0u;
+                    left_free = true;
+                }
+            }
+            return kNoRun;
+        }
+
         /* allocPageBasedSingleRegion's search (Scatter.hpp:775-813) for concurrent
-         * callers, without the global mutex. The chunk-size words are read 16 pages
-         * at a time (independent loads issued together, not one round trip per
-         * page), free runs are counted exactly as the reference counts them
-         * (downward, reset at a used page), and markpages' CAS decides who owns a
-         * run. A lane that loses a run to a concurrent claim keeps counting the
-         * free pages its markpages had held below the lost page, so no hole is
-         * left between its next run and the winner's. The hint is updated as the
-         * reference updates it: lowered to
+         * callers, without the global mutex. It visits the pages the reference
+         * visits, startpage down to endpage, and counts free runs as the
+         * reference counts them (downward, reset at a used page), but reads the
+         * free-page bitmap: 16 words, 512 pages, per round trip, with whole
+         * words of free or used pages taken in one step. markpages' CAS on the
+         * chunk sizes decides who owns a run. A lane that loses a run to a
+         * concurrent claim keeps counting the free pages its markpages had held
+         * below the lost page, so no hole is left between its next run and the
+         * winner's. The hint is updated as the reference updates it: lowered to
          * just below the run by a CAS from the value the search started at, when
          * the search passed no used page. With no concurrent caller this finds
          * the reference's run. */
         __device__ __forceinline__ char* alloc_page_based_scan(const PageScan& c, u32 startpage, u32 endpage,
                                                                u32 bytes)
         {
-            const u32 pagestoalloc = divup(bytes, c.pagesize);
-            u32 freecount = 0;
+            const u32 n = divup(bytes, c.pagesize);
+            u32 freecount = 0u;
             bool left_free = false;
-            /* the reference visits startpage down to endpage, both included
-             * (Scatter.hpp:785-787); pages top-1, top-2, ..., endpage remain */
+            const u32 wend = endpage >> 5;
+            /* pages top-1, top-2, ..., endpage remain (top wraps to 0 for the
+             * reference's underflowed hint: then nothing is visited); a start
+             * past page numpages, which no consistent hint holds, is cut to it
+             * so every bitmap word read lies inside the map */
+            if(startpage > c.numpages && startpage != 0xFFFFFFFFu)
+                startpage = c.numpages;
             u32 top = startpage + 1u;
             while(top > endpage)
             {
-                const u32 lo = (top - endpage > 16u) ? top - 16u : endpage;
-                MMC_STAT_ADD(c, MMC_STAT_PAGE_SCAN, top - lo);
-                u32 v[16];
+                const u32 whi = (top - 1u) >> 5;
+                const u32 g0 = whi & ~3u; /* 16-byte group holding word whi */
+                uint4 grp[4];
 #pragma unroll
-                for(u32 k = 0; k < 16u; ++k)
-                {
-                    const u32 q = top - 1u - k;
-                    v[k] = (q >= lo && q < c.numpages) ? __ldcg(&c.chunksize[q]) : 1u;
-                }
+                for(u32 k = 0; k < 4u; ++k)
+                    grp[k] = (g0 >= 4u * k && g0 - 4u * k + 3u >= wend)
+                                 ? __ldcg(reinterpret_cast<const uint4*>(c.freemap + (g0 - 4u * k)))
+                                 : make_uint4(0u, 0u, 0u, 0u);
+                u32 q = kNoRun;
+                u32 wl = whi; /* lowest word scanned */
 #pragma unroll
-                for(u32 k = 0; k < 16u; ++k)
+                for(u32 j = 0; j < 16u; ++j)
                 {
-                    const u32 q = top - 1u - k;
-                    if(q < lo)
+                    if(g0 + 3u < j)
+                        break; /* below word 0 */
+                    const u32 w = g0 + 3u - j;
+                    if(w > whi)
+                        continue;
+                    if(w < wend)
                         break;
-                    if(v[k] == 0u)
-                    {
-                        if(++freecount == pagestoalloc)
-                        {
-                            u32 free_below = 0u;
-                            if(q + pagestoalloc <= c.numpages
-                               && markpages_batched(c, q, pagestoalloc, bytes, free_below))
-                            {
-                                if(!left_free)
-                                {
-                                    /* the reference stores q - 1, which wraps for a run
-                                     * ending at page 0 (Scatter.hpp:800-804) and leaves
-                                     * every later search empty; fixed mode stores 0 */
-                                    const u32 nf = (!c.reference_quirks && q == 0u) ? 0u : q - 1u;
-                                    atomicCAS(&c.state->firstFreePageBased, startpage, nf);
-                                }
-                                return c.pages + static_cast<u64>(q) * c.pagesize;
-                            }
-                            MMC_STAT(c, MMC_STAT_PAGE_LOST);
-                            /* the run below the lost page is still free: keep counting it */
-                            freecount = free_below;
-                            left_free = true;
-                        }
-                    }
-                    else
-                    {
-                        left_free = true;
-                        freecount = 0u;
-                    }
+                    const uint4 G = grp[j / 4u];
+                    const u32 comp = 3u - (j % 4u);
+                    const u32 x = comp == 3u ? G.w : (comp == 2u ? G.z : (comp == 1u ? G.y : G.x));
+                    wl = w;
+                    q = scan_freemap_word(x, w, w == whi ? ((top - 1u) & 31u) : 31u, w == wend ? (endpage & 31u) : 0u,
+                                          n, freecount, left_free);
+                    if(q != kNoRun)
+                        break;
                 }
-                top = lo;
+                MMC_STAT_ADD(c, MMC_STAT_PAGE_SCAN, 32u * (whi - wl + 1u));
+                if(q == kNoRun)
+                {
+                    top = wl == wend ? endpage : 32u * wl;
+                    continue;
+                }
+                u32 free_below = 0u;
+                if(q + n <= c.numpages && markpages_batched(c, q, n, bytes, free_below))
+                {
+                    if(!left_free)
+                    {
+                        /* the reference stores q - 1, which wraps for a run
+                         * ending at page 0 (Scatter.hpp:800-804) and leaves
+                         * every later search empty; fixed mode stores 0 */
+                        const u32 nf = (!c.reference_quirks && q == 0u) ? 0u : q - 1u;
+                        atomicCAS(&c.state->firstFreePageBased, startpage, nf);
+                    }
+                    return c.pages + static_cast<u64>(q) * c.pagesize;
+                }
+                MMC_STAT(c, MMC_STAT_PAGE_LOST);
+                /* the run below the lost page is still free: keep counting it,
+                 * from the page below q */
+                freecount = free_below;
+                left_free = true;
+                top = q;
             }
             return nullptr;
         }
@@ -981,7 +1099,7 @@ namespace mmc
             if(Ids::warpSize == 1u)
                 return alloc_page_based_single(h, bytes);
             return alloc_page_based_concurrent(
-                PageScan{h.chunksize, h.state, h.pages, h.numpages, h.pagesize, h.reference_quirks}, bytes);
+                PageScan{h.chunksize, h.freemap, h.state, h.pages, h.numpages, h.pagesize, h.reference_quirks}, bytes);
         }
 
         /* deallocPageBased, Scatter.hpp:874-886 (out of line, as the search) */
@@ -994,6 +1112,7 @@ namespace mmc
             __threadfence();
             for(u32 p = page; p < end; ++p)
                 atomicCAS(&h.chunksize[p], bytes, 0u);
+            freemap_range(h.freemap, page, end - page, true);
             atomicMax(&h.state->firstFreePageBased, page + pages - 1u);
         }
 

@@ -108,6 +108,9 @@ typedef struct mmc_device_handle
     uint32_t* count;     /* per-page fill count (word 1) */
     uint32_t* bitmask;   /* per-page chunk / segment bitmask (word 2) */
     uint32_t* regions;   /* per-region fill counters */
+    uint32_t* freemap;   /* free-page bitmap: bit (i & 31) of word i >> 5 is set while page i
+                            has chunk size 0 (heap-owned, outside the pool; read by the
+                            concurrent multi-page search) */
     uint32_t numpages;
     uint32_t numregions;
     uint32_t accessblocks;
@@ -228,6 +231,12 @@ mmc_status mmc_heap_error(mmc_heap* heap, void* stream, uint32_t* flags, int cle
  * (pages tried by walks, regions skipped, multi-page words scanned); they have no counterpart
  * in the reference and are maintained only in MMC_DEVICE_STATS builds. */
 mmc_status mmc_heap_stats(mmc_heap* heap, void* stream, unsigned long long* out, int clear);
+
+/* Copy the free-page bitmap to a host buffer of (numpages + 31) / 32 words
+ * (bit i & 31 of word i >> 5: page i has chunk size 0). Waits for `stream`.
+ * No counterpart in the reference (whose multi-page search reads the page
+ * table itself). */
+mmc_status mmc_snapshot_freemap(mmc_heap* heap, void* stream, uint32_t* words);
 
 /* Copy the metadata to host buffers (each may be NULL): ptes3 = numpages x
  * {chunksize, count, bitmask}; regions = numregions words; masks = numpages x

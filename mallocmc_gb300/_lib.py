@@ -32,7 +32,7 @@ class MmcConfig(ctypes.Structure):
 class MmcDeviceHandle(ctypes.Structure):
     _fields_ = [
         ("state", vp), ("pages", vp), ("chunksize", vp), ("count", vp), ("bitmask", vp), ("regions", vp),
-        ("numpages", u32), ("numregions", u32), ("accessblocks", u32), ("pagesperblock", u32),
+        ("freemap", vp), ("numpages", u32), ("numregions", u32), ("accessblocks", u32), ("pagesperblock", u32),
         ("pagesize", u32), ("regionsize", u32), ("wastefactor", u32), ("resetfreedpages", u32),
         ("hashingK", u32), ("hashingDistMP", u32), ("hashingDistWP", u32), ("hashingDistWPRel", u32),
         ("dataAlignment", u32), ("distribution", u32), ("oom_policy", u32), ("reference_quirks", u32),
@@ -93,6 +93,7 @@ SIGNATURES = {
                                                    vp, vp]),
     "mmc_heap_error": (ctypes.c_int, [vp, vp, ctypes.POINTER(u32), ctypes.c_int]),
     "mmc_snapshot_metadata": (ctypes.c_int, [vp, vp, vp, vp, vp, vp]),
+    "mmc_snapshot_freemap": (ctypes.c_int, [vp, vp, vp]),
     "mmc_heap_stats": (ctypes.c_int, [vp, vp, vp, ctypes.c_int]),
     "mmc_last_error": (ctypes.c_char_p, []),
     "mmc_run_program": (ctypes.c_int, [vp, vp, vp, i64, vp, vp]),

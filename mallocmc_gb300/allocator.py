@@ -132,3 +132,12 @@ class Allocator:
                 "snapshot")
         return ptes, regions, masks[:, : g.maxOnPageMasks], {
             "firstFreePageBased": int(hdr[0]), "firstfreeblock": int(hdr[1]), "pagebasedMutex": int(hdr[2])}
+
+    def freemap(self, stream=None) -> np.ndarray:
+        """The free-page bitmap as one bool per page (True: the bit is set,
+        i.e. the page counts as free for the concurrent multi-page search)."""
+        g = self.geometry()
+        words = np.zeros((g.numpages + 31) // 32, dtype=np.uint32)
+        L.check(L.lib().mmc_snapshot_freemap(self._h, _stream_ptr(stream), words.ctypes.data), "snapshot_freemap")
+        bits = np.unpackbits(words.view(np.uint8), bitorder="little")
+        return bits[: g.numpages].astype(bool)

@@ -50,6 +50,8 @@ struct mmc_heap
     char* pool;       /* after Shrink::alignPool */
     size_t memsize;
     char* devblock;   /* mmc_heap_state + slot partials + result word */
+    uint32_t* freemap; /* free-page bitmap (mmc_device_handle::freemap) */
+    size_t freemap_words; /* words allocated */
     mmc_heap_state* state;
     SlotPartial* partials;
     unsigned* result_word;
@@ -96,8 +98,17 @@ using mmc::dev::RunSum;
 /* initDeviceFunction's zeroing (Scatter.hpp:1026-1032) for the page tails, and
  * the header words (:1034-1044). The page-table and region arrays are zeroed
  * with cudaMemsetAsync before this kernel. */
-__global__ void mmc_init_kernel(mmc_device_handle h)
+__global__ void mmc_init_kernel(mmc_device_handle h, uint32_t freemap_words)
 {
+    /* every page starts free: its bit set; bits past numpages stay clear, so
+     * the multi-page search sees them (and page numpages) as used */
+    for(uint32_t w = blockIdx.x * blockDim.x + threadIdx.x; w < freemap_words; w += gridDim.x * blockDim.x)
+    {
+        const uint32_t first = w * 32u;
+        h.freemap[w] = first >= h.numpages ? 0u
+                                           : (h.numpages - first >= 32u ? 0xFFFFFFFFu
+                                                                         : (1u << (h.numpages - first)) - 1u);
+    }
     const uint32_t n = h.maxOnPageMasks;
     const uint64_t total = static_cast<uint64_t>(h.numpages) * n;
     for(uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; i < total;
@@ -354,6 +365,7 @@ namespace
         d.count = d.chunksize + g.numpages;
         d.bitmask = d.count + g.numpages;
         d.regions = reinterpret_cast<uint32_t*>(h->pool + g.regions_offset);
+        d.freemap = h->freemap;
         d.numpages = g.numpages;
         d.numregions = g.numregions;
         d.accessblocks = g.accessblocks;
@@ -389,11 +401,31 @@ namespace
         }
     }
 
+    /* words of the free-page bitmap: one bit per page and a clear bit for page
+     * numpages, rounded up to whole 16-byte groups (the search reads four
+     * words at a time) and one spare group */
+    size_t freemap_words_for(uint32_t numpages) { return ((static_cast<size_t>(numpages) / 32u + 1u + 3u) & ~size_t{3}) + 4u; }
+
     mmc_status init_heap(mmc_heap* h, cudaStream_t s)
     {
         mmc_status st = compute_geometry(h->cfg, h->pool, h->memsize, &h->geom);
         if(st != MMC_OK)
             return st;
+        const size_t fm_words = freemap_words_for(h->geom.numpages);
+        if(fm_words > h->freemap_words)
+        {
+            if(h->freemap)
+                cudaFree(h->freemap);
+            h->freemap = nullptr;
+            h->freemap_words = 0;
+            if(cudaMalloc(&h->freemap, fm_words * 4u) != cudaSuccess)
+            {
+                cudaGetLastError();
+                h->freemap = nullptr;
+                return fail(MMC_ERR_OOM, "cudaMalloc of the free-page bitmap failed");
+            }
+            h->freemap_words = fm_words;
+        }
         fill_handle(h);
         const mmc_geometry& g = h->geom;
         st = cuda_check(cudaMemsetAsync(h->pool + g.ptes_offset, 0, 12ull * g.numpages + 4ull * g.numregions, s),
@@ -405,7 +437,7 @@ namespace
         const uint64_t words = static_cast<uint64_t>(g.numpages) * g.maxOnPageMasks;
         const unsigned grid = static_cast<unsigned>(
             std::max<uint64_t>(1u, std::min<uint64_t>((words + 255u) / 256u, scan_grid(h->device) * 8u)));
-        mmc_init_kernel<<<grid, 256, 0, s>>>(h->handle);
+        mmc_init_kernel<<<grid, 256, 0, s>>>(h->handle, static_cast<uint32_t>(h->freemap_words));
         return cuda_check(cudaGetLastError(), "heap init kernel");
     }
 
@@ -556,6 +588,8 @@ mmc_status mmc_heap_destroy(mmc_heap* h)
         cudaFree(h->pool_raw);
     if(h->devblock)
         cudaFree(h->devblock);
+    if(h->freemap)
+        cudaFree(h->freemap);
     if(h->host_result)
         cudaFreeHost(h->host_result);
     delete h;
@@ -752,6 +786,18 @@ mmc_status mmc_heap_stats(mmc_heap* h, void* stream, unsigned long long* out, in
                         "copy stats");
     if(st == MMC_OK && clear)
         st = cuda_check(cudaMemset(h->state->stats, 0, sizeof(unsigned long long) * MMC_STAT_COUNT), "clear stats");
+    return st;
+}
+
+mmc_status mmc_snapshot_freemap(mmc_heap* h, void* stream, uint32_t* words)
+{
+    if(h == nullptr || words == nullptr)
+        return fail(MMC_ERR_ARG, "null argument");
+    cudaStream_t s = as_stream(stream);
+    const size_t n = (static_cast<size_t>(h->geom.numpages) + 31u) / 32u;
+    mmc_status st = cuda_check(cudaStreamSynchronize(s), "synchronise before freemap snapshot");
+    if(st == MMC_OK)
+        st = cuda_check(cudaMemcpy(words, h->freemap, n * 4u, cudaMemcpyDeviceToHost), "copy freemap");
     return st;
 }
 

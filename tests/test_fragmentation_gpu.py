@@ -59,6 +59,7 @@ def test_fill_reaches_the_reference(heap):
         assert alloc.error_flags() == 0
         assert r["released_live_bytes"] == 0
         assert_all_free(alloc.snapshot())
+        assert np.all(alloc.freemap()[alloc.snapshot()[0][:, 0] == 0])
         ptes = alloc.snapshot()[0]
         # no page-based run is left claimed: a page is either unformatted or a formatted chunk page
         assert int(np.count_nonzero(ptes[:, 0] > 4096)) == 0

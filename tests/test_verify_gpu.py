@@ -360,3 +360,69 @@ def test_page_based_hint_after_a_run_at_page_zero(quirks):
         assert want[:runs].tolist() == offs.tolist()
         assert int(want[-1]) == again
         assert alloc.error_flags() == 0
+
+
+def assert_freemap_consistent(alloc, max_false_positive=0.001):
+    """The free-page bitmap against the page table: every page whose chunk size
+    is 0 has its bit (a missed free page would hide runs from the multi-page
+    search); a set bit on a used page (a free's late set) is allowed, rarely."""
+    ptes = alloc.snapshot()[0]
+    bits = alloc.freemap()
+    free = ptes[:, 0] == 0
+    assert not np.any(free & ~bits), f"{int((free & ~bits).sum())} free pages without their bit"
+    assert int((bits & ~free).sum()) <= max(2, max_false_positive * len(free))
+
+
+def test_freemap_tracks_the_page_table():
+    """After chunked allocations (which format pages), concurrent multi-page
+    allocations, their frees and a fill to out-of-memory, the bitmap the
+    concurrent search reads agrees with the chunk sizes; after everything is
+    freed, every page is free in both."""
+    from mallocmc_gb300.workloads import alloc_offsets, free_offsets
+
+    cfg = HeapConfig(4096, 16 << 20, 16, 2, False)
+    rng = np.random.default_rng(5)
+    with gpu_allocator(cfg, 128 << 20) as alloc:
+        g = alloc.geometry()
+        assert np.all(alloc.freemap())
+        n = 8 * 128
+        sizes = np.where(rng.random(n) < 0.5, 16 * rng.integers(1, 200, size=n),
+                         16 * rng.integers(300, 20000, size=n)).astype(np.uint32)
+        ds, offs_t = alloc_offsets(alloc, 8, 128, sizes, 3)
+        offs = offs_t.cpu().numpy()
+        check_live_blocks(offs, sizes, g.numpages, 4096)
+        assert_freemap_consistent(alloc)
+        assert free_offsets(alloc, 8, 128, ds, offs_t, 3) == 0
+        assert_freemap_consistent(alloc)
+        ptes = alloc.snapshot()[0]
+        assert int(np.count_nonzero(ptes[:, 0] > 4096)) == 0
+        # multi-page runs only, more than fit: some fail; then free what was allocated
+        big = (16 * rng.integers(4096 // 16, (1 << 20) // 16, size=512)).astype(np.uint32)
+        ds, offs_t = alloc_offsets(alloc, 4, 128, big, 4)
+        offs = offs_t.cpu().numpy()
+        assert (offs < 0).any() and (offs >= 0).any()
+        check_live_blocks(offs, big, g.numpages, 4096)
+        assert_freemap_consistent(alloc)
+        assert free_offsets(alloc, 4, 128, ds, offs_t, 4) == 0
+        assert_freemap_consistent(alloc)
+        assert alloc.error_flags() == 0
+
+
+def test_freemap_with_page_resets():
+    """resetfreedpages: pages return to chunk size 0 when their last chunk is
+    freed, and their bits come back."""
+    from mallocmc_gb300.workloads import alloc_offsets, free_offsets
+
+    cfg = HeapConfig(4096, 16 << 20, 16, 2, True)
+    rng = np.random.default_rng(6)
+    with gpu_allocator(cfg, 64 << 20) as alloc:
+        for rnd in range(3):
+            n = 16 * 256
+            sizes = (16 * rng.integers(1, 128, size=n)).astype(np.uint32)
+            ds, offs_t = alloc_offsets(alloc, 16, 256, sizes, rnd)
+            assert_freemap_consistent(alloc)
+            assert free_offsets(alloc, 16, 256, ds, offs_t, rnd) == 0
+            assert_freemap_consistent(alloc)
+        ptes = alloc.snapshot()[0]
+        assert int(np.count_nonzero(ptes[:, 0])) == 0
+        assert np.all(alloc.freemap())
