@@ -927,14 +927,29 @@ namespace mmc
                     lost |= (old[k] != 0u ? 1u : 0u) << k;
                 if(lost != 0u)
                 {
+                    u32 top_back = 0u; /* highest page put back, plus one */
                     for(u32 trypage = startpage; trypage < base; ++trypage)
                         if(atomicCAS(&c.chunksize[trypage], bytes, 0u) == bytes)
+                        {
                             freemap_set(c.freemap, trypage);
+                            top_back = trypage + 1u;
+                        }
 #pragma unroll
                     for(u32 k = 0; k < 4u; ++k)
                         if(base + k < end && ((lost >> k) & 1u) == 0u
                            && atomicCAS(&c.chunksize[base + k], bytes, 0u) == bytes)
+                        {
                             freemap_set(c.freemap, base + k);
+                            top_back = base + k + 1u;
+                        }
+                    /* Pages put back are freed pages, and a free raises the
+                     * search hint over them (deallocPageBased's atomicMax,
+                     * Scatter.hpp:885): while this claim held them, concurrent
+                     * searches saw them used and may have settled below them
+                     * and lowered the hint, which would leave them a hole no
+                     * later search visits. */
+                    if(top_back != 0u)
+                        atomicMax(&c.state->firstFreePageBased, top_back - 1u);
                     /* the pages from startpage up to the lowest lost one were free */
                     free_below = base + static_cast<u32>(__ffs(static_cast<int>(lost))) - 1u - startpage;
                     return false;
@@ -950,7 +965,15 @@ namespace mmc
         /* Bits b_hi down to b_lo of free-page word w (value x), continuing a
          * downward count of consecutive free pages: returns the first page of
          * a run of n free pages once the count reaches n, else kNoRun. A used
-         * page resets the count and marks the search as having passed one. */
+         * page resets the count; one that ends a stretch of free pages the
+         * search could not use marks those pages as left behind (left_free),
+         * which keeps the search from lowering the hint past them. (The
+         * reference marks every used page, so its hint also stays above
+         * stretches of used pages it passed. Lowering it past those spares
+         * every later search the rescan and moves no placement while the pages
+         * stay used; a run freed there raises the hint again. Only a chunk
+         * page reset to free there under resetfreedpages, which raises no
+         * hint, is then found by the search from the top instead.) */
         __device__ __forceinline__ u32 scan_freemap_word(u32 x, u32 w, u32 b_hi, u32 b_lo, u32 n, u32& freecount,
                                                          bool& left_free)
         {
@@ -966,8 +989,8 @@ namespace mmc
             }
             if(xm == 0u)
             {
+                left_free = left_free || freecount != 0u;
                 freecount = 0u;
-                left_free = true;
                 return kNoRun;
             }
             for(u32 b = b_hi + 1u; b-- > b_lo;)
@@ -979,8 +1002,8 @@ namespace mmc
                 }
                 else
                 {
+                    left_free = left_free || freecount != 0u;
                     freecount = 0u;
-                    left_free = true;
                 }
             }
             return kNoRun;
@@ -995,10 +1018,11 @@ namespace mmc
          * chunk sizes decides who owns a run. A lane that loses a run to a
          * concurrent claim keeps counting the free pages its markpages had held
          * below the lost page, so no hole is left between its next run and the
-         * winner's. The hint is updated as the reference updates it: lowered to
-         * just below the run by a CAS from the value the search started at, when
-         * the search passed no used page. With no concurrent caller this finds
-         * the reference's run. */
+         * winner's, and puts the hint back over the pages it held, so they are
+         * searched again. The hint is lowered as the reference lowers it, to
+         * just below the run by a CAS from the value the search started at,
+         * when the search left no free page behind. With no concurrent caller
+         * this finds the reference's run. */
         __device__ __forceinline__ char* alloc_page_based_scan(const PageScan& c, u32 startpage, u32 endpage,
                                                                u32 bytes)
         {
