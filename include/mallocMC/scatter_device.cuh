@@ -961,6 +961,9 @@ namespace mmc
         }
 
         constexpr u32 kNoRun = 0xFFFFFFFFu;
+        /* lost runs a concurrent multi-page search looks at again before it
+         * settles below them */
+        constexpr u32 kLostRunRetries = 8u;
 
         /* Bits b_hi down to b_lo of free-page word w (value x), continuing a
          * downward count of consecutive free pages: returns the first page of
@@ -1019,7 +1022,8 @@ namespace mmc
          * concurrent claim keeps counting the free pages its markpages had held
          * below the lost page, so no hole is left between its next run and the
          * winner's, and puts the hint back over the pages it held, so they are
-         * searched again. The hint is lowered as the reference lowers it, to
+         * searched again; before that it looks at a lost run again a few times,
+         * since the claim that beat it may be put back too. The hint is lowered as the reference lowers it, to
          * just below the run by a CAS from the value the search started at,
          * when the search left no free page behind. With no concurrent caller
          * this finds the reference's run. */
@@ -1029,6 +1033,7 @@ namespace mmc
             const u32 n = divup(bytes, c.pagesize);
             u32 freecount = 0u;
             bool left_free = false;
+            u32 retries = 0u;
             const u32 wend = endpage >> 5;
             /* pages top-1, top-2, ..., endpage remain (top wraps to 0 for the
              * reference's underflowed hint: then nothing is visited); a start
@@ -1088,6 +1093,22 @@ namespace mmc
                     return c.pages + static_cast<u64>(q) * c.pagesize;
                 }
                 MMC_STAT(c, MMC_STAT_PAGE_LOST);
+                if(retries < kLostRunRetries)
+                {
+                    /* Look at the run's pages again, after a short backoff:
+                     * the claim that beat this one may itself lose elsewhere
+                     * and put its pages back, and two searches that take each
+                     * other's pages both lose. Going on below the lost page at
+                     * once would leave the top of the contested stretch to a
+                     * later search that may never come (a hole of a page or
+                     * two among the runs); the page above the run is used (or
+                     * above the start), so counting restarts from 0 there. */
+                    __nanosleep(64u << umin(retries, 4u));
+                    ++retries;
+                    top = q + n;
+                    freecount = 0u;
+                    continue;
+                }
                 /* the run below the lost page is still free: keep counting it,
                  * from the page below q */
                 freecount = free_below;
