@@ -34,6 +34,7 @@
 #include <stdexcept>
 #include <string>
 #include <tuple>
+#include <type_traits>
 #include <vector>
 
 /* version.hpp:40-47 */
@@ -311,6 +312,21 @@ namespace mallocMC
         size_t size;
     };
 
+    namespace detail
+    {
+        /* Scatter's resetfreedpages as 0/1; 0 for creation policies without one */
+        template<typename T, typename = void>
+        struct ResetOf
+        {
+            static constexpr uint32_t value = 0u;
+        };
+        template<typename T>
+        struct ResetOf<T, std::void_t<decltype(T::resetfreedpages)>>
+        {
+            static constexpr uint32_t value = T::resetfreedpages ? 1u : 0u;
+        };
+    } // namespace detail
+
     /* AllocatorHandleImpl (mallocMC_allocator_handle.hpp:35-63): passed to
      * kernels by value; all heap constants ride in kernel parameter space. */
     template<typename T_HostAllocator>
@@ -318,13 +334,22 @@ namespace mallocMC
     {
         mmc_device_handle devAllocator;
 
+        /* The thread ids with the allocator's policy values fixed at compile
+         * time, as the reference's templates fix them: only the code of this
+         * configuration is compiled into the user's kernels. */
+        using Ids = mmc::dev::GpuIdsFixed<
+            detail::ResetOf<typename T_HostAllocator::CreationPolicy>::value,
+            T_HostAllocator::DistributionPolicy::code,
+            T_HostAllocator::OOMPolicy::code,
+            static_cast<uint32_t>(T_HostAllocator::AlignmentPolicy::dataAlignment)>;
+
         AllocatorHandleImpl() = default;
         explicit AllocatorHandleImpl(mmc_device_handle const& h) : devAllocator(h) {}
 
         __device__ auto malloc(size_t size) -> void*
         {
             if constexpr(T_HostAllocator::CreationPolicy::usesHeap)
-                return mmc::dev::malloc<mmc::dev::GpuIds>(devAllocator, size);
+                return mmc::dev::malloc<Ids>(devAllocator, size);
             else
                 return ::malloc(static_cast<size_t>(static_cast<uint32_t>(size))); /* OldMalloc.hpp:56-60 */
         }
@@ -337,7 +362,7 @@ namespace mallocMC
         __device__ void free(void* p)
         {
             if constexpr(T_HostAllocator::CreationPolicy::usesHeap)
-                mmc::dev::free<mmc::dev::GpuIds>(devAllocator, p);
+                mmc::dev::free<Ids>(devAllocator, p);
             else
                 ::free(p); /* OldMalloc.hpp:62-66 */
         }
@@ -352,7 +377,7 @@ namespace mallocMC
         __device__ auto getAvailableSlots(size_t slotSize) -> unsigned
         {
             if constexpr(T_HostAllocator::CreationPolicy::providesAvailableSlots)
-                return mmc::dev::available_slots<mmc::dev::GpuIds>(devAllocator, slotSize);
+                return mmc::dev::available_slots<Ids>(devAllocator, slotSize);
             else
                 return 0u;
         }

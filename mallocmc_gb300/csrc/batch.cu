@@ -79,6 +79,7 @@ namespace
         return (s + 15u) & ~15u;
     }
 
+    template<class Ids>
     __device__ __forceinline__ void run_job_thread(const mmc_device_handle& h, const mmc_job& j, uint32_t jt,
                                                    unsigned long long& pairs, unsigned long long& nulls,
                                                    unsigned long long& bad, unsigned long long& csum)
@@ -90,7 +91,7 @@ namespace
         {
             const uint64_t m = mix64(j.seed, jt, c);
             const uint32_t bytes = draw_size(j, m, logq);
-            char* ptr = static_cast<char*>(dv::malloc<dv::GpuIds>(h, bytes));
+            char* ptr = static_cast<char*>(dv::malloc<Ids>(h, bytes));
             if(ptr == nullptr)
             {
                 ++nulls;
@@ -106,7 +107,7 @@ namespace
                 bad += (v.x != m + 2u * i) + (v.y != m + 2u * i + 1u);
                 csum += v.x ^ v.y;
             }
-            dv::free<dv::GpuIds>(h, ptr);
+            dv::free<Ids>(h, ptr);
             ++pairs;
         }
     }
@@ -139,6 +140,7 @@ namespace
 } // namespace
 
 /* Plain form: one launch per job. */
+template<class Ids>
 __global__ void __launch_bounds__(256) mmc_job_kernel(mmc_device_handle h, const mmc_job* jobs, uint32_t job,
                                                       unsigned long long* stats)
 {
@@ -146,7 +148,7 @@ __global__ void __launch_bounds__(256) mmc_job_kernel(mmc_device_handle h, const
     const uint32_t jt = blockIdx.x * blockDim.x + threadIdx.x;
     unsigned long long pairs = 0, nulls = 0, bad = 0, csum = 0;
     if(jt < j.threads)
-        run_job_thread(h, j, jt, pairs, nulls, bad, csum);
+        run_job_thread<Ids>(h, j, jt, pairs, nulls, bad, csum);
     flush_stats(stats + 4ull * job, pairs, nulls, bad, csum);
 }
 
@@ -161,7 +163,7 @@ __global__ void __launch_bounds__(256) mmc_job_kernel(mmc_device_handle h, const
  * adds to the global table once at its end; without, and for the rare null and
  * pattern-error counts, straight to the global table. (One thread's flush to
  * L2 is two atomics, more than its share of the allocations' atomics.) */
-template<bool SHARED_ROWS>
+template<bool SHARED_ROWS, class Ids>
 __global__ void __launch_bounds__(256) mmc_batch_kernel(mmc_device_handle h, const mmc_job* jobs, uint32_t njobs,
                                                         unsigned long long total_slots, unsigned long long* counter,
                                                         unsigned long long* stats)
@@ -257,7 +259,7 @@ __global__ void __launch_bounds__(256) mmc_batch_kernel(mmc_device_handle h, con
         {
             const uint64_t m = mix64(seed, jt, c);
             const uint32_t bytes = draw_size(j, m, logq);
-            char* ptr = static_cast<char*>(dv::malloc<dv::GpuIds>(h, bytes));
+            char* ptr = static_cast<char*>(dv::malloc<Ids>(h, bytes));
             if(ptr == nullptr)
                 ++nulls;
             else
@@ -272,7 +274,7 @@ __global__ void __launch_bounds__(256) mmc_batch_kernel(mmc_device_handle h, con
                     bad += (v.x != m + 2u * i) + (v.y != m + 2u * i + 1u);
                     csum += v.x ^ v.y;
                 }
-                dv::free<dv::GpuIds>(h, ptr);
+                dv::free<Ids>(h, ptr);
                 ++pairs;
             }
             ++c;
@@ -317,12 +319,11 @@ namespace
         cudaMemsetAsync(b->counter, 0, sizeof(unsigned long long), s);
         const unsigned long long slots = static_cast<unsigned long long>(b->total_items) * kItemThreads;
         const size_t rows_bytes = (sizeof(unsigned long long) + sizeof(uint32_t)) * b->njobs;
-        if(b->shared_rows)
-            mmc_batch_kernel<true><<<b->blocks, kItemThreads, rows_bytes, s>>>(b->handle, b->jobs, b->njobs, slots,
-                                                                                b->counter, b->stats);
-        else
-            mmc_batch_kernel<false><<<b->blocks, kItemThreads, 0, s>>>(b->handle, b->jobs, b->njobs, slots,
-                                                                        b->counter, b->stats);
+        MMC_DISPATCH_IDS(b->handle, if(b->shared_rows) mmc_batch_kernel<true, Ids>
+                                        <<<b->blocks, kItemThreads, rows_bytes, s>>>(b->handle, b->jobs, b->njobs,
+                                                                                     slots, b->counter, b->stats);
+                         else mmc_batch_kernel<false, Ids><<<b->blocks, kItemThreads, 0, s>>>(
+                             b->handle, b->jobs, b->njobs, slots, b->counter, b->stats));
     }
 } // namespace
 
@@ -422,7 +423,7 @@ mmc_status mmc_batch_run_plain(mmc_batch* b, void* stream)
     for(uint32_t i = 0; i < b->njobs; ++i)
     {
         const uint32_t grid = (b->host_jobs[i].threads + kItemThreads - 1u) / kItemThreads;
-        mmc_job_kernel<<<grid, kItemThreads, 0, s>>>(b->handle, b->jobs, i, b->stats);
+        MMC_DISPATCH_IDS(b->handle, mmc_job_kernel<Ids><<<grid, kItemThreads, 0, s>>>(b->handle, b->jobs, i, b->stats));
     }
     return cuda_check(cudaGetLastError(), "plain job kernels");
 }

@@ -9,6 +9,25 @@
 
 #include <string>
 
+/* Run the statements in __VA_ARGS__ with `Ids` naming the thread-id type the
+ * heap's kernels are launched with: GpuIdsDefault (the policy values fixed at
+ * compile time) when the handle holds the default configuration, GpuIds (read
+ * from the handle) otherwise. */
+#define MMC_DISPATCH_IDS(handle, ...)                                                                                 \
+    do                                                                                                                 \
+    {                                                                                                                  \
+        if(mmc::dev::GpuIdsDefault::matches(handle))                                                                   \
+        {                                                                                                              \
+            using Ids = mmc::dev::GpuIdsDefault;                                                                       \
+            __VA_ARGS__;                                                                                               \
+        }                                                                                                              \
+        else                                                                                                           \
+        {                                                                                                              \
+            using Ids = mmc::dev::GpuIds;                                                                              \
+            __VA_ARGS__;                                                                                               \
+        }                                                                                                              \
+    } while(0)
+
 namespace mmc
 {
     namespace host

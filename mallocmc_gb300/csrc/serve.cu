@@ -142,6 +142,7 @@ __global__ void mmc_serve_apply(mmc_serve_slot* slots, mmc_serve_slot* mirror, c
 }
 
 /* Grow one live request by `step` elements (one warp), completing it at its length. */
+template<class Ids>
 __device__ __forceinline__ void grow_request(const mmc_device_handle& h, mmc_serve_slot& s, void** chunks,
                                              uint32_t max_chunks, uint32_t step)
 {
@@ -154,7 +155,7 @@ __device__ __forceinline__ void grow_request(const mmc_device_handle& h, mmc_ser
     const uint32_t last_chunk = (end + kElemsPerChunk - 1u) / kElemsPerChunk; /* exclusive */
     for(uint32_t c = first_chunk + lane; c < last_chunk && c < max_chunks; c += 32u)
     {
-        void* p = dv::malloc<dv::GpuIds>(h, kChunkBytes);
+        void* p = dv::malloc<Ids>(h, kChunkBytes);
         chunks[c] = p;
         failed += p == nullptr;
     }
@@ -173,7 +174,7 @@ __device__ __forceinline__ void grow_request(const mmc_device_handle& h, mmc_ser
         /* give back what this step took; the request retries next tick */
         for(uint32_t c = first_chunk + lane; c < last_chunk && c < max_chunks; c += 32u)
             if(chunks[c])
-                dv::free<dv::GpuIds>(h, chunks[c]);
+                dv::free<Ids>(h, chunks[c]);
     }
     __syncwarp();
     if(lane == 0u)
@@ -200,7 +201,7 @@ __device__ __forceinline__ void grow_request(const mmc_device_handle& h, mmc_ser
             sum += __shfl_down_sync(0xFFFFFFFFu, sum, off);
         __syncwarp();
         for(uint32_t c = lane; c < last_chunk; c += 32u)
-            dv::free<dv::GpuIds>(h, chunks[c]);
+            dv::free<Ids>(h, chunks[c]);
         if(lane == 0u)
         {
             s.checksum = sum;
@@ -213,6 +214,7 @@ __device__ __forceinline__ void grow_request(const mmc_device_handle& h, mmc_ser
  * table. With `done` (pipelined ticks), a request that completes here is also
  * appended to the completion list, and each request still live adds the chunks
  * it will yet take to counts[1] (counts[0] is the list's length). */
+template<class Ids>
 __global__ void __launch_bounds__(256) mmc_serve_tick_kernel(mmc_device_handle h, mmc_serve_slot* slots,
                                                              mmc_serve_slot* mirror, void** chunks, uint32_t nslots,
                                                              uint32_t max_chunks, uint32_t step,
@@ -223,7 +225,7 @@ __global__ void __launch_bounds__(256) mmc_serve_tick_kernel(mmc_device_handle h
     {
         if(slots[w].state != MMC_SERVE_LIVE)
             continue;
-        grow_request(h, slots[w], chunks + static_cast<uint64_t>(w) * max_chunks, max_chunks, step);
+        grow_request<Ids>(h, slots[w], chunks + static_cast<uint64_t>(w) * max_chunks, max_chunks, step);
         __syncwarp();
         if((threadIdx.x & 31u) == 0u)
         {
@@ -265,12 +267,13 @@ __global__ void mmc_serve_publish(const mmc_serve_done* done, unsigned long long
 }
 
 /* Per-request form: one warp, one slot. */
+template<class Ids>
 __global__ void mmc_serve_one_kernel(mmc_device_handle h, mmc_serve_slot* slots, mmc_serve_slot* mirror,
                                      void** chunks, uint32_t slot, uint32_t max_chunks, uint32_t step)
 {
     if(slots[slot].state != MMC_SERVE_LIVE)
         return;
-    grow_request(h, slots[slot], chunks + static_cast<uint64_t>(slot) * max_chunks, max_chunks, step);
+    grow_request<Ids>(h, slots[slot], chunks + static_cast<uint64_t>(slot) * max_chunks, max_chunks, step);
     __syncwarp();
     if(threadIdx.x == 0u)
         mirror[slot] = slots[slot];
@@ -324,8 +327,9 @@ namespace
         if(batched)
         {
             const uint32_t blocks = (s->slots + 7u) / 8u;
-            mmc_serve_tick_kernel<<<blocks, 256, 0, st>>>(s->handle, s->d_slots, s->m_slots, s->d_chunks, s->slots,
-                                                         s->max_chunks, s->step, nullptr, nullptr);
+            MMC_DISPATCH_IDS(s->handle, mmc_serve_tick_kernel<Ids><<<blocks, 256, 0, st>>>(
+                                            s->handle, s->d_slots, s->m_slots, s->d_chunks, s->slots, s->max_chunks,
+                                            s->step, nullptr, nullptr));
         }
         mmc_status r = mmc_available_slots_async(s->heap, kChunkBytes, st, s->m_free);
         if(r != MMC_OK)
@@ -341,8 +345,9 @@ namespace
         mmc_serve_apply<<<8, 128, 0, st>>>(s->d_slots, s->m_slots, p.m_queue, p.m_queue_len, s->queue_cap, s->slots,
                                            &s->handle.state->error_flags);
         const uint32_t blocks = (s->slots + 7u) / 8u;
-        mmc_serve_tick_kernel<<<blocks, 256, 0, st>>>(s->handle, s->d_slots, s->m_slots, s->d_chunks, s->slots,
-                                                     s->max_chunks, s->step, p.d_done, p.d_counts);
+        MMC_DISPATCH_IDS(s->handle, mmc_serve_tick_kernel<Ids><<<blocks, 256, 0, st>>>(
+                                        s->handle, s->d_slots, s->m_slots, s->d_chunks, s->slots, s->max_chunks,
+                                        s->step, p.d_done, p.d_counts));
         mmc_status r = mmc_available_slots_async(s->heap, kChunkBytes, st, p.m_free);
         if(r != MMC_OK)
             return r;
@@ -594,8 +599,9 @@ mmc_status mmc_serve_tick(mmc_server* s, int batched)
                                                s->slots, &s->handle.state->error_flags);
         for(uint32_t w = 0; w < s->slots; ++w)
             if(live[w])
-                mmc_serve_one_kernel<<<1, 32, 0, stream>>>(s->handle, s->d_slots, s->m_slots, s->d_chunks, w,
-                                                           s->max_chunks, s->step);
+                MMC_DISPATCH_IDS(s->handle, mmc_serve_one_kernel<Ids><<<1, 32, 0, stream>>>(
+                                                s->handle, s->d_slots, s->m_slots, s->d_chunks, w, s->max_chunks,
+                                                s->step));
         st = mmc_available_slots_async(s->heap, kChunkBytes, stream, s->m_free);
         if(st == MMC_OK)
             st = cuda_check(cudaGetLastError(), "per-request tick");

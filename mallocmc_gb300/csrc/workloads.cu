@@ -143,7 +143,7 @@ __device__ __forceinline__ unsigned long long warp_pattern(char* ptr, uint32_t b
  * pattern, each verified block's whole cache lines are dropped from L2
  * (discard_dead_block) before it is freed: the block is dead, and its
  * payload would otherwise be written back to DRAM (6 % faster). */
-template<uint32_t PATTERN>
+template<uint32_t PATTERN, class Ids>
 __global__ void __launch_bounds__(256, 4) mmc_stress_kernel(mmc_device_handle h, mmc_stress_params p,
                                                          const uint16_t* sizes, unsigned long long* stats)
 {
@@ -156,7 +156,7 @@ __global__ void __launch_bounds__(256, 4) mmc_stress_kernel(mmc_device_handle h,
         const uint64_t m = mix64(p.seed, t, r);
         const uint32_t bytes
             = sizes ? sizes[r * nthreads + t] : p.lo + (static_cast<uint32_t>(m >> 32) % nsizes) * p.step;
-        char* ptr = static_cast<char*>(dv::malloc<dv::GpuIds>(h, bytes));
+        char* ptr = static_cast<char*>(dv::malloc<Ids>(h, bytes));
         if constexpr(PATTERN == MMC_PATTERN_WARP)
         {
             /* every lane takes part, with or without a block */
@@ -166,7 +166,7 @@ __global__ void __launch_bounds__(256, 4) mmc_stress_kernel(mmc_device_handle h,
             else
             {
                 /* the verified block is dead: its whole lines leave L2 unwritten */
-                dv::free<dv::GpuIds>(h, dv::discard_dead_block(ptr, bytes));
+                dv::free<Ids>(h, dv::discard_dead_block(ptr, bytes));
                 ++pairs;
             }
             continue;
@@ -190,7 +190,7 @@ __global__ void __launch_bounds__(256, 4) mmc_stress_kernel(mmc_device_handle h,
                 csum += v.x ^ v.y;
             }
         }
-        dv::free<dv::GpuIds>(h, ptr);
+        dv::free<Ids>(h, ptr);
         ++pairs;
     }
     /* warp-aggregate the counters */
@@ -314,6 +314,7 @@ __device__ __forceinline__ unsigned long long frag_check_tags(const char* p, uin
     return bad;
 }
 
+template<class Ids>
 __global__ void __launch_bounds__(256) mmc_fill_kernel(mmc_device_handle h, mmc_frag_params p, uint64_t wave,
                                                        void** ptrs, uint32_t* sizes, uint64_t capacity,
                                                        unsigned long long* counters)
@@ -323,7 +324,7 @@ __global__ void __launch_bounds__(256) mmc_fill_kernel(mmc_device_handle h, mmc_
     const uint64_t T = static_cast<uint64_t>(gridDim.x) * blockDim.x;
     const uint64_t t = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     const uint32_t size = frag_size(p, p.first_request + wave * T + t);
-    char* ptr = static_cast<char*>(dv::malloc<dv::GpuIds>(h, size));
+    char* ptr = static_cast<char*>(dv::malloc<Ids>(h, size));
     atomicAdd(&counters[2], 1ull);
     if(ptr == nullptr)
     {
@@ -333,7 +334,7 @@ __global__ void __launch_bounds__(256) mmc_fill_kernel(mmc_device_handle h, mmc_
     const unsigned long long slot = atomicAdd(&counters[0], 1ull);
     if(slot >= capacity)
     {
-        dv::free<dv::GpuIds>(h, ptr);
+        dv::free<Ids>(h, ptr);
         atomicExch(reinterpret_cast<unsigned*>(&counters[4]), 1u);
         return;
     }
@@ -343,6 +344,7 @@ __global__ void __launch_bounds__(256) mmc_fill_kernel(mmc_device_handle h, mmc_
     atomicAdd(&counters[1], static_cast<unsigned long long>(size));
 }
 
+template<class Ids>
 __global__ void mmc_free_list_kernel(mmc_device_handle h, void** ptrs, uint32_t* sizes, const uint32_t* idx,
                                      uint64_t n, unsigned long long* counters)
 {
@@ -356,7 +358,7 @@ __global__ void mmc_free_list_kernel(mmc_device_handle h, void** ptrs, uint32_t*
             continue;
         bad += frag_check_tags(ptr, sizes[s], s);
         bytes += sizes[s];
-        dv::free<dv::GpuIds>(h, ptr);
+        dv::free<Ids>(h, ptr);
         ptrs[s] = nullptr;
         sizes[s] = 0u;
     }
@@ -379,7 +381,7 @@ __global__ void mmc_verify_list_kernel(void* const* ptrs, const uint32_t* sizes,
 }
 
 /* Verify workload: malloc(sizes[t]); write u32 (t ^ seed); optionally verify and free. */
-template<bool ALLOC, bool FREE>
+template<bool ALLOC, bool FREE, class Ids>
 __global__ void mmc_verify_kernel(mmc_device_handle h, uint32_t nthreads, const uint32_t* sizes, uint32_t seed,
                                   int64_t* offsets, unsigned long long* errors)
 {
@@ -391,7 +393,7 @@ __global__ void mmc_verify_kernel(mmc_device_handle h, uint32_t nthreads, const 
     uint32_t* p = nullptr;
     if(ALLOC)
     {
-        p = static_cast<uint32_t*>(dv::malloc<dv::GpuIds>(h, sizes[t]));
+        p = static_cast<uint32_t*>(dv::malloc<Ids>(h, sizes[t]));
         offsets[t] = p ? static_cast<int64_t>(reinterpret_cast<char*>(p) - h.pages) : -1;
         if(p)
             for(uint32_t i = 0; i < sizes[t] / 4u; ++i)
@@ -410,7 +412,7 @@ __global__ void mmc_verify_kernel(mmc_device_handle h, uint32_t nthreads, const 
             bad += (p[i] != pattern);
         if(bad)
             atomicAdd(errors, bad);
-        dv::free<dv::GpuIds>(h, p);
+        dv::free<Ids>(h, p);
     }
 }
 
@@ -504,12 +506,10 @@ mmc_status mmc_run_stress(mmc_heap* heap, const mmc_stress_params* p, const uint
     mmc_device_handle h;
     mmc_heap_device_handle(heap, &h);
     /* one instantiation per pattern mode: only the mode's code is in the kernel */
-    if(p->write_pattern == MMC_PATTERN_WARP)
-        mmc_stress_kernel<MMC_PATTERN_WARP><<<p->blocks, p->threads_per_block, 0, as_stream(stream)>>>(h, *p, sizes,
-                                                                                                       stats);
-    else
-        mmc_stress_kernel<MMC_PATTERN_THREAD><<<p->blocks, p->threads_per_block, 0, as_stream(stream)>>>(h, *p, sizes,
-                                                                                                         stats);
+    MMC_DISPATCH_IDS(h, if(p->write_pattern == MMC_PATTERN_WARP) mmc_stress_kernel<MMC_PATTERN_WARP, Ids>
+                            <<<p->blocks, p->threads_per_block, 0, as_stream(stream)>>>(h, *p, sizes, stats);
+                     else mmc_stress_kernel<MMC_PATTERN_THREAD, Ids>
+                         <<<p->blocks, p->threads_per_block, 0, as_stream(stream)>>>(h, *p, sizes, stats));
     return cuda_check(cudaGetLastError(), "stress kernel");
 }
 
@@ -543,8 +543,8 @@ mmc_status mmc_run_verify(mmc_heap* heap, uint32_t blocks, uint32_t tpb, const u
         return fail(MMC_ERR_ARG, "bad argument");
     mmc_device_handle h;
     mmc_heap_device_handle(heap, &h);
-    mmc_verify_kernel<true, true><<<blocks, tpb, 0, as_stream(stream)>>>(h, blocks * tpb, sizes, seed, offsets,
-                                                                       errors);
+    MMC_DISPATCH_IDS(h, mmc_verify_kernel<true, true, Ids>
+                     <<<blocks, tpb, 0, as_stream(stream)>>>(h, blocks * tpb, sizes, seed, offsets, errors));
     return cuda_check(cudaGetLastError(), "verify kernel");
 }
 
@@ -555,8 +555,8 @@ mmc_status mmc_run_alloc_offsets(mmc_heap* heap, uint32_t blocks, uint32_t tpb, 
         return fail(MMC_ERR_ARG, "bad argument");
     mmc_device_handle h;
     mmc_heap_device_handle(heap, &h);
-    mmc_verify_kernel<true, false><<<blocks, tpb, 0, as_stream(stream)>>>(h, blocks * tpb, sizes, seed, offsets,
-                                                                        nullptr);
+    MMC_DISPATCH_IDS(h, mmc_verify_kernel<true, false, Ids>
+                     <<<blocks, tpb, 0, as_stream(stream)>>>(h, blocks * tpb, sizes, seed, offsets, nullptr));
     return cuda_check(cudaGetLastError(), "alloc kernel");
 }
 
@@ -567,8 +567,8 @@ mmc_status mmc_run_free_offsets(mmc_heap* heap, uint32_t blocks, uint32_t tpb, c
         return fail(MMC_ERR_ARG, "bad argument");
     mmc_device_handle h;
     mmc_heap_device_handle(heap, &h);
-    mmc_verify_kernel<false, true><<<blocks, tpb, 0, as_stream(stream)>>>(h, blocks * tpb, sizes, seed,
-                                                                        const_cast<int64_t*>(offsets), errors);
+    MMC_DISPATCH_IDS(h, mmc_verify_kernel<false, true, Ids><<<blocks, tpb, 0, as_stream(stream)>>>(
+                            h, blocks * tpb, sizes, seed, const_cast<int64_t*>(offsets), errors));
     return cuda_check(cudaGetLastError(), "free kernel");
 }
 
@@ -585,8 +585,8 @@ mmc_status mmc_run_fill(mmc_heap* heap, const mmc_frag_params* p, void** ptrs, u
     mmc_heap_device_handle(heap, &h);
     for(uint32_t w = 0; w < p->waves; ++w)
     {
-        mmc_fill_kernel<<<p->blocks, p->threads_per_block, 0, as_stream(stream)>>>(h, *p, w, ptrs, sizes, capacity,
-                                                                                   counters);
+        MMC_DISPATCH_IDS(h, mmc_fill_kernel<Ids><<<p->blocks, p->threads_per_block, 0, as_stream(stream)>>>(
+                                h, *p, w, ptrs, sizes, capacity, counters));
         const cudaError_t e = cudaGetLastError();
         if(e != cudaSuccess)
             return cuda_check(e, "fill kernel");
@@ -605,7 +605,7 @@ mmc_status mmc_run_free_list(mmc_heap* heap, void** ptrs, uint32_t* sizes, const
     mmc_device_handle h;
     mmc_heap_device_handle(heap, &h);
     const unsigned grid = static_cast<unsigned>(std::min<uint64_t>((n + 255u) / 256u, scan_grid(0) * 4u));
-    mmc_free_list_kernel<<<grid, 256, 0, as_stream(stream)>>>(h, ptrs, sizes, idx, n, counters);
+    MMC_DISPATCH_IDS(h, mmc_free_list_kernel<Ids><<<grid, 256, 0, as_stream(stream)>>>(h, ptrs, sizes, idx, n, counters));
     return cuda_check(cudaGetLastError(), "free-list kernel");
 }
 
