@@ -38,6 +38,7 @@ struct mmc_batch
     uint32_t threads_per_block;
     std::vector<mmc_job> host_jobs;
     mmc_job* jobs;              /* device copy, item_begin filled */
+    uint32_t* item_job;         /* job of each 256-thread work item (total_items entries) */
     unsigned long long* counter; /* job-thread counter of the persistent form */
     bool shared_rows;            /* per-block pair/checksum columns fit shared memory and u32 */
     unsigned long long* stats;  /* njobs x 4 */
@@ -156,7 +157,9 @@ __global__ void __launch_bounds__(256) mmc_job_kernel(mmc_device_handle h, const
  * slots [256 * item_begin_i, 256 * item_begin_i + threads_i); the slots up to
  * the next job's first item are padding and are skipped. Every lane runs one
  * job thread at a time, one cycle per pass of the loop; lanes that need a
- * thread take consecutive slots with one atomicAdd per warp. A lane's counters
+ * thread take consecutive slots with one atomicAdd per warp, and a table of
+ * each work item's job (built with the batch) names the slot's job in one
+ * load. A lane's counters
  * are flushed to its job's row when it leaves a thread. With SHARED_ROWS the
  * pairs and the checksum (the words every thread adds to) go to the block's
  * copy of those two columns in shared memory (12 B per job), which the block
@@ -164,7 +167,8 @@ __global__ void __launch_bounds__(256) mmc_job_kernel(mmc_device_handle h, const
  * pattern-error counts, straight to the global table. (One thread's flush to
  * L2 is two atomics, more than its share of the allocations' atomics.) */
 template<bool SHARED_ROWS, class Ids>
-__global__ void __launch_bounds__(256) mmc_batch_kernel(mmc_device_handle h, const mmc_job* jobs, uint32_t njobs,
+__global__ void __launch_bounds__(256) mmc_batch_kernel(mmc_device_handle h, const mmc_job* jobs,
+                                                        const uint32_t* item_job, uint32_t njobs,
                                                         unsigned long long total_slots, unsigned long long* counter,
                                                         unsigned long long* stats)
 {
@@ -228,17 +232,7 @@ __global__ void __launch_bounds__(256) mmc_batch_kernel(mmc_device_handle h, con
                 }
                 else
                 {
-                    const uint32_t item = static_cast<uint32_t>(slot / kItemThreads);
-                    uint32_t lo = 0, hi = njobs; /* last job whose first item <= item */
-                    while(hi - lo > 1u)
-                    {
-                        const uint32_t mid = (lo + hi) / 2u;
-                        if(jobs[mid].item_begin <= item)
-                            lo = mid;
-                        else
-                            hi = mid;
-                    }
-                    job = lo;
+                    job = item_job[static_cast<uint32_t>(slot / kItemThreads)];
                     j = jobs[job];
                     jt = static_cast<uint32_t>(slot - static_cast<unsigned long long>(j.item_begin) * kItemThreads);
                     if(jt < j.threads)
@@ -311,6 +305,8 @@ namespace
             cudaFree(b->counter);
         if(b->stats)
             cudaFree(b->stats);
+        if(b->item_job)
+            cudaFree(b->item_job);
         delete b;
     }
 
@@ -320,10 +316,11 @@ namespace
         const unsigned long long slots = static_cast<unsigned long long>(b->total_items) * kItemThreads;
         const size_t rows_bytes = (sizeof(unsigned long long) + sizeof(uint32_t)) * b->njobs;
         MMC_DISPATCH_IDS(b->handle, if(b->shared_rows) mmc_batch_kernel<true, Ids>
-                                        <<<b->blocks, kItemThreads, rows_bytes, s>>>(b->handle, b->jobs, b->njobs,
-                                                                                     slots, b->counter, b->stats);
+                                        <<<b->blocks, kItemThreads, rows_bytes, s>>>(b->handle, b->jobs, b->item_job,
+                                                                                     b->njobs, slots, b->counter,
+                                                                                     b->stats);
                          else mmc_batch_kernel<false, Ids><<<b->blocks, kItemThreads, 0, s>>>(
-                             b->handle, b->jobs, b->njobs, slots, b->counter, b->stats));
+                             b->handle, b->jobs, b->item_job, b->njobs, slots, b->counter, b->stats));
     }
 } // namespace
 
@@ -367,7 +364,21 @@ mmc_status mmc_batch_create(mmc_heap* heap, const mmc_job* jobs, uint32_t njobs,
             b->shared_rows = false; /* a block's pair count of the job could pass 32 bits */
     b->blocks = persistent_blocks ? persistent_blocks : scan_grid(b->device) * 2u;
     cudaStream_t s = as_stream(stream);
+    std::vector<uint32_t> item_job(b->total_items);
+    for(uint32_t i = 0; i < njobs; ++i)
+    {
+        const uint32_t end = i + 1u < njobs ? b->host_jobs[i + 1u].item_begin : b->total_items;
+        for(uint32_t it = b->host_jobs[i].item_begin; it < end; ++it)
+            item_job[it] = i;
+    }
     mmc_status st = cuda_check(cudaMalloc(&b->jobs, sizeof(mmc_job) * njobs), "cudaMalloc jobs");
+    if(st == MMC_OK)
+        st = cuda_check(cudaMalloc(&b->item_job, sizeof(uint32_t) * (b->total_items > 0u ? b->total_items : 1u)),
+                        "cudaMalloc item table");
+    if(st == MMC_OK && b->total_items > 0u)
+        st = cuda_check(cudaMemcpyAsync(b->item_job, item_job.data(), sizeof(uint32_t) * b->total_items,
+                                        cudaMemcpyHostToDevice, s),
+                        "copy item table");
     if(st == MMC_OK)
         st = cuda_check(cudaMalloc(&b->counter, sizeof(unsigned long long)), "cudaMalloc counter");
     if(st == MMC_OK)
