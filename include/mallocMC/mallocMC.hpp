@@ -364,7 +364,10 @@ namespace mallocMC
             if constexpr(T_HostAllocator::CreationPolicy::usesHeap)
                 mmc::dev::free<Ids>(devAllocator, p);
             else
-                ::free(p); /* OldMalloc.hpp:62-66 */
+            {
+                mmc::dev::release_fence(); /* the accesses before the free are performed first */
+                ::free(p);                 /* OldMalloc.hpp:62-66 */
+            }
         }
         template<typename AlpakaAcc>
         __device__ void free(AlpakaAcc const&, void* p)

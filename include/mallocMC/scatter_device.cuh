@@ -161,6 +161,9 @@ namespace mmc
         {
             asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
         }
+        /* fence.acq_rel.gpu: this thread's earlier memory operations are
+         * performed before its later ones, for every thread of the GPU */
+        __device__ __forceinline__ void release_fence() { asm volatile("fence.acq_rel.gpu;" ::: "memory"); }
         __device__ __forceinline__ u32 lanemask_lt()
         {
             u32 r;
@@ -1224,6 +1227,14 @@ namespace mmc
         {
             if(mem == nullptr)
                 return;
+            /* Release: every access this thread made to the block (and the
+             * lanes' accesses a __syncwarp before the call ordered before it)
+             * is performed before the atomics below hand the block to a next
+             * owner. The reference's free has no such fence; without it a
+             * thread's last reads of the block can be served after a next
+             * owner's writes (a per-thread write/verify/free stress on GB300
+             * read foreign data in 1 to 6 of 25 runs, none with the fence). */
+            release_fence();
             const u32 P = h.pagesize;
             const u64 offset = static_cast<u64>(static_cast<char*>(mem) - h.pages);
             if(offset >= static_cast<u64>(h.numpages) * P)
@@ -1379,18 +1390,17 @@ namespace mmc
          *
          * Why no later owner's data can be discarded. In the PTX memory model
          * a discard is a weak write of indeterminate bytes to each line. The
-         * fence.acq_rel.gpu after the discards orders them (and every earlier
-         * access of this thread to the block, including what other lanes of
-         * the warp wrote into it before a __syncwarp this thread passed)
-         * before every later memory operation of the thread: the free's
-         * chunk-size load and the relaxed device-scope atomics that release
-         * the chunk (a fence followed by a strong write is a release
-         * pattern). A later owner can reach the block only through an atomic
-         * that reads what those atomics wrote, and its accesses to the block
-         * take their address from that atomic's result, so they reach L2
-         * after the discards. The fence waits for L2 to acknowledge the
-         * discards; a dependent read of each discarded line, the other way to
-         * order them, misses L2 and measured 17 % slower on the stress. */
+         * free that follows starts with a fence.acq_rel.gpu, which orders the
+         * discards (and every earlier access of this thread to the block,
+         * including what other lanes of the warp wrote into it before a
+         * __syncwarp this thread passed) before the relaxed device-scope
+         * atomics that release the chunk: a fence followed by a strong write
+         * is a release pattern. A later owner can reach the block only
+         * through an atomic that reads what those atomics wrote, and its
+         * accesses to the block take their address from that atomic's result,
+         * so they reach L2 after the discards. (A dependent read of each
+         * discarded line, the other way to order them, misses L2 and measured
+         * 17 % slower on the stress.) Call it right before the free. */
         __device__ __forceinline__ void* discard_dead_block(void* p, u32 bytes)
         {
             const u64 a = reinterpret_cast<u64>(p);
@@ -1398,7 +1408,6 @@ namespace mmc
             const u64 end = a + bytes;
             for(u64 x = lo; x + 128ull <= end; x += 128ull)
                 asm volatile("discard.global.L2 [%0], 128;" ::"l"(x) : "memory");
-            asm volatile("fence.acq_rel.gpu;" ::: "memory");
             return p;
         }
 

@@ -233,7 +233,11 @@ __global__ void __launch_bounds__(256) mmc_stress_oldmalloc_kernel(mmc_stress_pa
                 ++nulls;
             else
             {
-                ::free(dv::discard_dead_block(ptr, bytes)); /* as the GB300 heap's stress does */
+                /* as the GB300 heap's stress does; CUDA's free is given the
+                 * same release fence the Scatter free issues itself */
+                dv::discard_dead_block(ptr, bytes);
+                dv::release_fence();
+                ::free(ptr);
                 ++pairs;
             }
             continue;
@@ -256,6 +260,7 @@ __global__ void __launch_bounds__(256) mmc_stress_oldmalloc_kernel(mmc_stress_pa
                 csum += v.x ^ v.y;
             }
         }
+        dv::release_fence();
         ::free(ptr);
         ++pairs;
     }

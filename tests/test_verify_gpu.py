@@ -426,3 +426,23 @@ def test_freemap_with_page_resets():
         ptes = alloc.snapshot()[0]
         assert int(np.count_nonzero(ptes[:, 0])) == 0
         assert np.all(alloc.freemap())
+
+
+def test_free_orders_the_threads_accesses_before_reuse():
+    """Sixteen full-grid runs of per-thread write / verify / free on a 1 GiB
+    heap: no thread may read another owner's data in its own block. Before the
+    free issued a release fence, a thread's verify reads could be served after
+    the next owner's writes (1 to 6 of 25 such runs found mismatches)."""
+    import torch
+
+    from mallocmc_gb300.workloads import PATTERN_THREAD, run_stress
+
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    cfg = HeapConfig(4096, 64 << 20, 16, 2, False)
+    bad = 0
+    for rep in range(16):
+        with gpu_allocator(cfg, 1 << 30) as alloc:
+            st = run_stress(alloc, sms * 4, 256, 20, 16, 1024, 16, seed=100 + rep, write_pattern=PATTERN_THREAD)
+            assert st["pairs"] == sms * 4 * 256 * 20 and st["nulls"] == 0
+            bad += st["bad"]
+    assert bad == 0
