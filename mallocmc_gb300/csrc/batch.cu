@@ -165,9 +165,11 @@ __global__ void __launch_bounds__(256) mmc_job_kernel(mmc_device_handle h, const
  * copy of those two columns in shared memory (12 B per job), which the block
  * adds to the global table once at its end; without, and for the rare null and
  * pattern-error counts, straight to the global table. (One thread's flush to
- * L2 is two atomics, more than its share of the allocations' atomics.) */
+ * L2 is two atomics, more than its share of the allocations' atomics.) Four
+ * resident blocks per SM (64 registers, a few spilled) against three at the
+ * unbounded 80: 7 % faster on the tuned geometry, 4.5 % on the defaults. */
 template<bool SHARED_ROWS, class Ids>
-__global__ void __launch_bounds__(256) mmc_batch_kernel(mmc_device_handle h, const mmc_job* jobs,
+__global__ void __launch_bounds__(256, 4) mmc_batch_kernel(mmc_device_handle h, const mmc_job* jobs,
                                                         const uint32_t* item_job, uint32_t njobs,
                                                         unsigned long long total_slots, unsigned long long* counter,
                                                         unsigned long long* stats)
