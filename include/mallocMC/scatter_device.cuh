@@ -1008,9 +1008,12 @@ namespace mmc
         /* Bits b_hi down to b_lo of free-page word w (value x), continuing a
          * downward count of consecutive free pages: returns the first page of
          * a run of n free pages once the count reaches n, else kNoRun. A used
-         * page resets the count; one that ends a stretch of free pages the
-         * search could not use marks those pages as left behind (left_free),
-         * which keeps the search from lowering the hint past them. (The
+         * page resets the count; one that ends a stretch of two or more free
+         * pages the search could not use marks those pages as left behind
+         * (left_free), which keeps the search from lowering the hint past
+         * them. A single free page between used ones is not counted: no
+         * multi-page run (two pages at least) can use it until a neighbour is
+         * freed, and that free raises the hint again. (The
          * reference marks every used page, so its hint also stays above
          * stretches of used pages it passed. Lowering it past those spares
          * every later search the rescan and moves no placement while the pages
@@ -1032,7 +1035,7 @@ namespace mmc
             }
             if(xm == 0u)
             {
-                left_free = left_free || freecount != 0u;
+                left_free = left_free || freecount > 1u;
                 freecount = 0u;
                 return kNoRun;
             }
@@ -1045,7 +1048,7 @@ namespace mmc
                 }
                 else
                 {
-                    left_free = left_free || freecount != 0u;
+                    left_free = left_free || freecount > 1u;
                     freecount = 0u;
                 }
             }
