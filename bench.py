@@ -178,7 +178,7 @@ STRESS_DRAM_BYTES_PER_PAIR = 166.0
 STRESS_NCU_ATOMICS_PER_PAIR = 3.93
 # L2 atomic requests per pair of the batched workload's persistent kernel, from
 # an ncu capture on the tuned geometry (profiles/mmc_batch_kernel_512jobs_4GiB.md).
-BATCH_NCU_ATOMICS_PER_PAIR = 0.206
+BATCH_NCU_ATOMICS_PER_PAIR = 0.211
 STRESS_TRAFFIC_NOTE = ("dram__bytes_read.sum + dram__bytes_write.sum per pair from an ncu capture of the same "
                        "kernel on a 2 GiB heap / 20 rounds, times the pairs of one launch")
 

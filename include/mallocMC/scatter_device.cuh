@@ -74,6 +74,9 @@ namespace mmc
             /* read the racy first-free-block hint through L1 (it changes rarely
              * and a stale value only moves where the search starts) */
             static constexpr bool cachedHints = true;
+            /* requests above a page take the multi-page path (SmallRequests
+             * leaves it out) */
+            static constexpr bool pageBased = true;
             __device__ static __forceinline__ u32 laneid()
             {
                 u32 r;
@@ -126,12 +129,28 @@ namespace mmc
          * use: no page reset, XMallocSIMD, ReturnNull, Shrink<16>. */
         using GpuIdsDefault = GpuIdsFixed<0u, MMC_DIST_XMALLOCSIMD, MMC_OOM_RETURNNULL, 16u>;
 
+        /* Base for a kernel whose requests never exceed a page after padding
+         * (its caller knows the largest one): the multi-page search is left
+         * out of it. That search is out-of-line code, and ptxas fits the
+         * registers of every kernel that can call it around the search's own,
+         * so a change in the search moved the chunk paths' register
+         * allocation: the uniform stress kernel, which never asks for more
+         * than 1 KiB, ran 2 to 17 % slower after changes to the search alone.
+         * A request above a page in such a kernel returns NULL and sets
+         * MMC_DEVERR_PAGEBASED. Frees are unchanged. */
+        template<class Base>
+        struct SmallRequests : Base
+        {
+            static constexpr bool pageBased = false;
+        };
+
         /* The reference's CPU-backend semantics (mallocMC_utils.hpp:85-87, 99-101, 121-123, 134-136). */
         struct SerialIds
         {
             static constexpr u32 warpSize = 1u;
             static constexpr bool coalesce = false; /* XMallocSIMD.hpp:136-137 */
             static constexpr bool cachedHints = false;
+            static constexpr bool pageBased = true;
             __device__ static __forceinline__ u32 laneid() { return 0u; }
             __device__ static __forceinline__ u32 warpid() { return 0u; }
             __device__ static __forceinline__ u32 smid() { return 0u; }
@@ -161,9 +180,12 @@ namespace mmc
         {
             asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
         }
-        /* fence.acq_rel.gpu: this thread's earlier memory operations are
-         * performed before its later ones, for every thread of the GPU */
-        __device__ __forceinline__ void release_fence() { asm volatile("fence.acq_rel.gpu;" ::: "memory"); }
+        /* fence.release.gpu: this thread's earlier memory operations are
+         * performed before its later writes and atomics, for every thread of
+         * the GPU. (It measured 6 % faster on the uniform stress than
+         * fence.acq_rel.gpu, which also orders the later reads; the free
+         * needs only the release.) */
+        __device__ __forceinline__ void release_fence() { asm volatile("fence.release.gpu;" ::: "memory"); }
         __device__ __forceinline__ u32 lanemask_lt()
         {
             u32 r;
@@ -944,23 +966,37 @@ namespace mmc
             u32 reference_quirks;
         };
 
-        /* markpages (Scatter.hpp:745-764) for concurrent callers: the CASes go
-         * out 4 at a time (independent atomics in flight together, not one
-         * round trip per page); on a failure every page this call set is put
-         * back with CAS(bytes -> 0), as the reference's roll-back does, and
-         * gets its free-page bit back. A run that is marked has its bits
-         * cleared (and the clears performed) before it is handed out. With no
-         * concurrent caller the outcome is the serial form's. */
+        /* markpages (Scatter.hpp:745-764) for concurrent callers. The run's
+         * top page is claimed first, alone: searches that meet one free
+         * stretch all settle on runs ending at its top page, and that CAS lets
+         * exactly one of them go on, while the others lose it holding no page
+         * (a claim that lost part way would put back pages that concurrent
+         * searches saw taken and settled below, leaving a hole of a page or
+         * two that no multi-page run fits). The other pages' CASes go out 4 at
+         * a time (independent atomics in flight together, not one round trip
+         * per page); on a failure every page this call set is put back with
+         * CAS(bytes -> 0), as the reference's roll-back does, and gets its
+         * free-page bit back. A run that is marked has its bits cleared (and
+         * the clears performed) before it is handed out. With no concurrent
+         * caller the outcome is the serial form's, which claims upward. */
         __device__ __forceinline__ bool markpages_batched(const PageScan& c, u32 startpage, u32 pages, u32 bytes,
-                                                          u32& free_below)
+                                                          u32& free_below, u32& top_owner)
         {
             const u32 end = startpage + pages;
-            for(u32 base = startpage; base < end; base += 4u)
+            top_owner = atomicCAS(&c.chunksize[end - 1u], 0u, bytes);
+            if(top_owner != 0u)
+            {
+                /* the pages below the top were free in the search */
+                free_below = pages - 1u;
+                return false;
+            }
+            const u32 last = end - 1u;
+            for(u32 base = startpage; base < last; base += 4u)
             {
                 u32 old[4];
 #pragma unroll
                 for(u32 k = 0; k < 4u; ++k)
-                    old[k] = (base + k < end) ? atomicCAS(&c.chunksize[base + k], 0u, bytes) : 0u;
+                    old[k] = (base + k < last) ? atomicCAS(&c.chunksize[base + k], 0u, bytes) : 0u;
                 u32 lost = 0u;
 #pragma unroll
                 for(u32 k = 0; k < 4u; ++k)
@@ -968,19 +1004,24 @@ namespace mmc
                 if(lost != 0u)
                 {
                     u32 top_back = 0u; /* highest page put back, plus one */
+                    if(atomicCAS(&c.chunksize[last], bytes, 0u) == bytes)
+                    {
+                        freemap_set(c.freemap, last);
+                        top_back = end;
+                    }
                     for(u32 trypage = startpage; trypage < base; ++trypage)
                         if(atomicCAS(&c.chunksize[trypage], bytes, 0u) == bytes)
                         {
                             freemap_set(c.freemap, trypage);
-                            top_back = trypage + 1u;
+                            top_back = umax(top_back, trypage + 1u);
                         }
 #pragma unroll
                     for(u32 k = 0; k < 4u; ++k)
-                        if(base + k < end && ((lost >> k) & 1u) == 0u
+                        if(base + k < last && ((lost >> k) & 1u) == 0u
                            && atomicCAS(&c.chunksize[base + k], bytes, 0u) == bytes)
                         {
                             freemap_set(c.freemap, base + k);
-                            top_back = base + k + 1u;
+                            top_back = umax(top_back, base + k + 1u);
                         }
                     /* Pages put back are freed pages, and a free raises the
                      * search hint over them (deallocPageBased's atomicMax,
@@ -1061,15 +1102,19 @@ namespace mmc
          * reference counts them (downward, reset at a used page), but reads the
          * free-page bitmap: 16 words, 512 pages, per round trip, with whole
          * words of free or used pages taken in one step. markpages' CAS on the
-         * chunk sizes decides who owns a run. A lane that loses a run to a
-         * concurrent claim keeps counting the free pages its markpages had held
-         * below the lost page, so no hole is left between its next run and the
-         * winner's, and puts the hint back over the pages it held, so they are
-         * searched again; before that it looks at a lost run again a few times,
-         * since the claim that beat it may be put back too. The hint is lowered as the reference lowers it, to
-         * just below the run by a CAS from the value the search started at,
-         * when the search left no free page behind. With no concurrent caller
-         * this finds the reference's run. */
+         * chunk sizes decides who owns a run, top page first. A lane that
+         * loses the top page learns the winner's size from the CAS and goes on
+         * right below the winner's run (every search that met the same free
+         * stretch settled on a run ending at its top page), from the bitmap
+         * words it has already read: the lanes that meet one stretch together
+         * pack their runs into it one below the other, with no page left
+         * between them, as the reference's serial search would. A lane that
+         * loses a page below the top (a claim that settled elsewhere) looks
+         * at the run again a few times, since that claim may be put back,
+         * then keeps counting below the lost page. The hint is lowered as the
+         * reference lowers it, to just below the run by a CAS from the value
+         * the search started at, when the search left no free page behind.
+         * With no concurrent caller this finds the reference's run. */
         __device__ __forceinline__ char* alloc_page_based_scan(const PageScan& c, u32 startpage, u32 endpage,
                                                                u32 bytes)
         {
@@ -1085,19 +1130,29 @@ namespace mmc
             if(startpage > c.numpages && startpage != 0xFFFFFFFFu)
                 startpage = c.numpages;
             u32 top = startpage + 1u;
+            u32 g0 = 0u;
+            uint4 grp[4];
+            bool reuse = false; /* the window read last still holds word whi */
             while(top > endpage)
             {
                 const u32 whi = (top - 1u) >> 5;
-                const u32 g0 = whi & ~3u; /* 16-byte group holding word whi */
-                uint4 grp[4];
+                if(!(reuse && whi <= g0 + 3u && whi + 12u >= g0))
+                {
+                    g0 = whi & ~3u; /* 16-byte group holding word whi */
 #pragma unroll
-                for(u32 k = 0; k < 4u; ++k)
-                    grp[k] = (g0 >= 4u * k && g0 - 4u * k + 3u >= wend)
-                                 ? __ldcg(reinterpret_cast<const uint4*>(c.freemap + (g0 - 4u * k)))
-                                 : make_uint4(0u, 0u, 0u, 0u);
+                    for(u32 k = 0; k < 4u; ++k)
+                        grp[k] = (g0 >= 4u * k && g0 - 4u * k + 3u >= wend)
+                                     ? __ldcg(reinterpret_cast<const uint4*>(c.freemap + (g0 - 4u * k)))
+                                     : make_uint4(0u, 0u, 0u, 0u);
+                }
+                reuse = false;
                 u32 q = kNoRun;
                 u32 wl = whi; /* lowest word scanned */
-#pragma unroll
+                /* Not unrolled: ptxas fits the registers of every kernel that
+                 * calls malloc around this out-of-line search's own, and the
+                 * unrolled loop (the window held in registers) made the
+                 * uniform stress kernel spill and run 17 % slower. */
+#pragma unroll 1
                 for(u32 j = 0; j < 16u; ++j)
                 {
                     if(g0 + 3u < j)
@@ -1122,8 +1177,8 @@ namespace mmc
                     top = wl == wend ? endpage : 32u * wl;
                     continue;
                 }
-                u32 free_below = 0u;
-                if(q + n <= c.numpages && markpages_batched(c, q, n, bytes, free_below))
+                u32 free_below = 0u, top_owner = 0u;
+                if(q + n <= c.numpages && markpages_batched(c, q, n, bytes, free_below, top_owner))
                 {
                     if(!left_free)
                     {
@@ -1136,6 +1191,20 @@ namespace mmc
                     return c.pages + static_cast<u64>(q) * c.pagesize;
                 }
                 MMC_STAT(c, MMC_STAT_PAGE_LOST);
+                if(top_owner != 0u)
+                {
+                    /* The run's top page went to a concurrent claim: a chunk
+                     * page, or a run of top_owner bytes, which in the common
+                     * case ends at that page (the searches that meet one free
+                     * stretch settle on runs ending at its top). Go on below
+                     * it, without waiting for its claim to show in the map. */
+                    const u32 skip = top_owner > c.pagesize ? divup(top_owner, c.pagesize) : 1u;
+                    const u32 qt = q + n; /* lost top page, plus one */
+                    top = qt > skip ? qt - skip : 0u;
+                    freecount = 0u;
+                    reuse = true;
+                    continue;
+                }
                 if(retries < kLostRunRetries)
                 {
                     /* Look at the run's pages again, after a short backoff:
@@ -1212,8 +1281,16 @@ namespace mmc
                 return nullptr;
             if(bytes <= h.pagesize)
                 return alloc_chunked<Ids>(h, bytes);
-            MMC_STAT(h, MMC_STAT_PAGE_BASED);
-            return alloc_page_based<Ids>(h, bytes);
+            if constexpr(!Ids::pageBased)
+            {
+                set_error(h, MMC_DEVERR_PAGEBASED);
+                return nullptr;
+            }
+            else
+            {
+                MMC_STAT(h, MMC_STAT_PAGE_BASED);
+                return alloc_page_based<Ids>(h, bytes);
+            }
         }
 
         /* 64-bit division for page sizes that are not powers of two, kept out of line */
@@ -1224,20 +1301,21 @@ namespace mmc
 
         /* destroy, Scatter.hpp:918-946. A pointer outside the pool or on a page
          * without a chunk size (where the reference would divide by zero) is
-         * recorded as MMC_DEVERR_BADFREE and ignored. */
+         * recorded as MMC_DEVERR_BADFREE and ignored.
+         *
+         * Release: every access this thread made to the block is performed
+         * before the atomics that hand the block to a next owner, by a release
+         * fence ahead of them. Every lane fences before the lanes that free
+         * parts of one chunk meet at a __syncwarp, so each lane's accesses to
+         * its part are performed before the one grouped decrement. The reference's free has no such
+         * fence; without it a thread's last reads of the block can be served
+         * after a next owner's writes (a per-thread write/verify/free stress on
+         * GB300 read foreign data in 1 to 6 of 25 runs, none with the fence). */
         template<class Ids>
         __device__ void destroy(const mmc_device_handle& h, void* mem)
         {
             if(mem == nullptr)
                 return;
-            /* Release: every access this thread made to the block (and the
-             * lanes' accesses a __syncwarp before the call ordered before it)
-             * is performed before the atomics below hand the block to a next
-             * owner. The reference's free has no such fence; without it a
-             * thread's last reads of the block can be served after a next
-             * owner's writes (a per-thread write/verify/free stress on GB300
-             * read foreign data in 1 to 6 of 25 runs, none with the fence). */
-            release_fence();
             const u32 P = h.pagesize;
             const u64 offset = static_cast<u64>(static_cast<char*>(mem) - h.pages);
             if(offset >= static_cast<u64>(h.numpages) * P)
@@ -1247,7 +1325,11 @@ namespace mmc
             }
             const u32 page = (P & (P - 1u)) == 0u ? static_cast<u32>(offset >> (__ffs(static_cast<int>(P)) - 1))
                                                   : page_of_offset_slow(offset, P);
+            /* The page's chunk size cannot change while this thread holds a
+             * block on it: it is loaded first, and its round trip overlaps the
+             * release fence's wait below instead of following it. */
             const u32 chunksize = ld_rlx(&h.chunksize[page]);
+            release_fence();
             if(chunksize == 0u)
             {
                 set_error(h, MMC_DEVERR_BADFREE);
@@ -1260,10 +1342,9 @@ namespace mmc
             {
                 /* XMallocSIMD sub-allocation: the lane count lives at the chunk head.
                  * Lanes freeing parts of the same chunk together subtract as one
-                 * (the lowest of them, after a __syncwarp that orders every
-                 * peer's accesses to its part before the decrement); whoever
-                 * takes the count to zero frees the chunk, as each lane's own
-                 * decrement would. */
+                 * (the lowest of them, after a __syncwarp that every lane
+                 * reaches after its own release fence); whoever takes the count
+                 * to zero frees the chunk, as each lane's own decrement would. */
                 u32* counter = reinterpret_cast<u32*>(page_data(h, page) + block * chunksize);
                 u32 sub = 1u;
                 if constexpr(Ids::warpSize > 1u)
@@ -1393,12 +1474,11 @@ namespace mmc
          *
          * Why no later owner's data can be discarded. In the PTX memory model
          * a discard is a weak write of indeterminate bytes to each line. The
-         * free that follows starts with a fence.acq_rel.gpu, which orders the
-         * discards (and every earlier access of this thread to the block,
-         * including what other lanes of the warp wrote into it before a
-         * __syncwarp this thread passed) before the relaxed device-scope
-         * atomics that release the chunk: a fence followed by a strong write
-         * is a release pattern. A later owner can reach the block only
+         * free that follows issues a fence.release.gpu in every lane ahead of
+         * the relaxed device-scope atomics that release the chunk, which
+         * orders the discards (and every earlier access of the thread to the
+         * block) before those atomics: a fence followed by a strong write is
+         * a release pattern. A later owner can reach the block only
          * through an atomic that reads what those atomics wrote, and its
          * accesses to the block take their address from that atomic's result,
          * so they reach L2 after the discards. (A dependent read of each

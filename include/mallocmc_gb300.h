@@ -51,6 +51,8 @@ typedef enum mmc_status
 #define MMC_DEVERR_OOM 0x4u      /* an allocation failed under MMC_OOM_FLAG */
 #define MMC_DEVERR_BADCMD 0x8u   /* a serving tick skipped a command (slot beyond the table, unknown kind)
                                     or cut a queue length beyond the queue's capacity */
+#define MMC_DEVERR_PAGEBASED 0x10u /* a request above a page in a kernel built without the multi-page path
+                                      (mmc::dev::SmallRequests: a batch whose job sizes fit a page, for one) */
 
 /* Device event counters (mmc_heap_stats); maintained only when the library is
  * built with MMC_DEVICE_STATS, zero otherwise. */
@@ -264,9 +266,10 @@ mmc_status mmc_run_program(mmc_heap* heap, const uint8_t* kinds, const uint64_t*
                            void* stream);
 
 /* Uniform stress (every thread `rounds` x {malloc(size), write a u64 pattern,
- * verify it, free}). Sizes: sizes[t * rounds + r] (u16, bytes) if sizes != NULL,
- * else drawn from seed uniformly in {lo, lo+step, ..., hi}. stats (device, 4 x u64,
- * accumulated, caller zeroes): {pairs, nulls, pattern errors, checksum}. */
+ * verify it, free}). Sizes: sizes[r * T + t] (u16, bytes; T = blocks x
+ * threads_per_block) if sizes != NULL, else drawn from seed uniformly in
+ * {lo, lo+step, ..., hi}. stats (device, 4 x u64, accumulated, caller zeroes):
+ * {pairs, nulls, pattern errors, checksum}. */
 typedef struct mmc_stress_params
 {
     uint32_t blocks;

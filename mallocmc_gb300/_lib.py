@@ -14,7 +14,7 @@ LIB_PATH = os.path.join(PKG, "libmallocmc_gb300.so")
 MMC_OK, MMC_ERR_CONFIG, MMC_ERR_CUDA, MMC_ERR_TIMEOUT, MMC_ERR_OOM, MMC_ERR_ARG = range(6)
 MMC_DIST_NOOP, MMC_DIST_XMALLOCSIMD = 0, 1
 MMC_OOM_RETURNNULL, MMC_OOM_FLAG = 0, 1
-MMC_DEVERR_TIMEOUT, MMC_DEVERR_BADFREE, MMC_DEVERR_OOM, MMC_DEVERR_BADCMD = 0x1, 0x2, 0x4, 0x8
+MMC_DEVERR_TIMEOUT, MMC_DEVERR_BADFREE, MMC_DEVERR_OOM, MMC_DEVERR_BADCMD, MMC_DEVERR_PAGEBASED = 0x1, 0x2, 0x4, 0x8, 0x10
 MMC_SERVE_FREE, MMC_SERVE_LIVE, MMC_SERVE_DONE = 0, 1, 2
 
 u32, u64, i64, vp = ctypes.c_uint32, ctypes.c_uint64, ctypes.c_int64, ctypes.c_void_p

@@ -41,6 +41,7 @@ struct mmc_batch
     uint32_t* item_job;         /* job of each 256-thread work item (total_items entries) */
     unsigned long long* counter; /* job-thread counter of the persistent form */
     bool shared_rows;            /* per-block pair/checksum columns fit shared memory and u32 */
+    uint32_t max_request;        /* the largest max_size of the jobs (a request's bytes before padding) */
     unsigned long long* stats;  /* njobs x 4 */
     cudaGraph_t graph;
     cudaGraphExec_t exec;
@@ -317,7 +318,7 @@ namespace
         cudaMemsetAsync(b->counter, 0, sizeof(unsigned long long), s);
         const unsigned long long slots = static_cast<unsigned long long>(b->total_items) * kItemThreads;
         const size_t rows_bytes = (sizeof(unsigned long long) + sizeof(uint32_t)) * b->njobs;
-        MMC_DISPATCH_IDS(b->handle, if(b->shared_rows) mmc_batch_kernel<true, Ids>
+        MMC_DISPATCH_IDS_SIZED(b->handle, b->max_request, if(b->shared_rows) mmc_batch_kernel<true, Ids>
                                         <<<b->blocks, kItemThreads, rows_bytes, s>>>(b->handle, b->jobs, b->item_job,
                                                                                      b->njobs, slots, b->counter,
                                                                                      b->stats);
@@ -353,6 +354,7 @@ mmc_status mmc_batch_create(mmc_heap* heap, const mmc_job* jobs, uint32_t njobs,
         }
         j.item_begin = static_cast<uint32_t>(items);
         items += (j.threads + kItemThreads - 1u) / kItemThreads;
+        b->max_request = std::max(b->max_request, j.max_size);
     }
     if(items > 0xFFFFFFF0ull)
     {
@@ -436,7 +438,8 @@ mmc_status mmc_batch_run_plain(mmc_batch* b, void* stream)
     for(uint32_t i = 0; i < b->njobs; ++i)
     {
         const uint32_t grid = (b->host_jobs[i].threads + kItemThreads - 1u) / kItemThreads;
-        MMC_DISPATCH_IDS(b->handle, mmc_job_kernel<Ids><<<grid, kItemThreads, 0, s>>>(b->handle, b->jobs, i, b->stats));
+        MMC_DISPATCH_IDS_SIZED(b->handle, b->host_jobs[i].max_size,
+                               mmc_job_kernel<Ids><<<grid, kItemThreads, 0, s>>>(b->handle, b->jobs, i, b->stats));
     }
     return cuda_check(cudaGetLastError(), "plain job kernels");
 }

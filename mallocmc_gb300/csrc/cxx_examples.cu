@@ -199,6 +199,26 @@ namespace
             h.free(acc, ar3);
     }
 
+    /* User code on the raw device API whose requests fit a page: the kernel
+     * is built with SmallRequests, which leaves the multi-page search out of
+     * it. Here one request above a page is made on purpose: it fails
+     * (nullptr, MMC_DEVERR_PAGEBASED), while the same request through the
+     * handle takes the multi-page path. */
+    __global__ void smallRequestsKernel(ScatterAllocator::AllocatorHandle h, int* out)
+    {
+        using Small = mmc::dev::SmallRequests<ScatterAllocator::AllocatorHandle::Ids>;
+        void* a = mmc::dev::malloc<Small>(h.devAllocator, 256);
+        void* b = mmc::dev::malloc<Small>(h.devAllocator, 3 * 4096 + 16);
+        void* c = h.malloc(3 * 4096 + 16);
+        out[0] = a != nullptr;
+        out[1] = b == nullptr;
+        out[2] = c != nullptr;
+        if(a != nullptr)
+            mmc::dev::free<Small>(h.devAllocator, a);
+        if(c != nullptr)
+            h.free(c);
+    }
+
     int report(const std::exception& e)
     {
         std::fprintf(stderr, "mmcx: %s\n", e.what());
@@ -326,6 +346,29 @@ int mmcx_oldmalloc(int device, int length, unsigned long long* sum, unsigned lon
         cudaFree(d_fail);
         cudaFree(d_sums);
         return e == cudaSuccess ? 0 : 2;
+    }
+    catch(const std::exception& e)
+    {
+        return report(e);
+    }
+}
+
+/* SmallRequests: out[3] = {the small request succeeded, the request above a
+ * page failed, the same request through the handle succeeded}; *flags the
+ * heap's device error bits afterwards. */
+int mmcx_small_requests(int device, int* out, unsigned* flags)
+{
+    try
+    {
+        cudaSetDevice(device);
+        ScatterAllocator alloc(device, nullptr, 256U * 1024U * 1024U);
+        int* d_out = nullptr;
+        cudaMalloc(&d_out, 3 * sizeof(int));
+        smallRequestsKernel<<<1, 1>>>(alloc.getAllocatorHandle(), d_out);
+        cudaMemcpy(out, d_out, 3 * sizeof(int), cudaMemcpyDeviceToHost);
+        *flags = alloc.errorFlags();
+        cudaFree(d_out);
+        return cudaDeviceSynchronize() == cudaSuccess ? 0 : 2;
     }
     catch(const std::exception& e)
     {

@@ -28,6 +28,33 @@
         }                                                                                                              \
     } while(0)
 
+/* As MMC_DISPATCH_IDS, for a launch whose largest request (bytes, before
+ * padding) the host knows: when it fits a page after padding, the default
+ * configuration's instance is the one without the multi-page path
+ * (mmc::dev::SmallRequests). */
+#define MMC_DISPATCH_IDS_SIZED(handle, max_request, ...)                                                              \
+    do                                                                                                                 \
+    {                                                                                                                  \
+        if(mmc::dev::GpuIdsDefault::matches(handle))                                                                   \
+        {                                                                                                              \
+            if(mmc::dev::apply_padding(16u, (max_request)) <= (handle).pagesize)                                      \
+            {                                                                                                          \
+                using Ids = mmc::dev::SmallRequests<mmc::dev::GpuIdsDefault>;                                          \
+                __VA_ARGS__;                                                                                           \
+            }                                                                                                          \
+            else                                                                                                       \
+            {                                                                                                          \
+                using Ids = mmc::dev::GpuIdsDefault;                                                                   \
+                __VA_ARGS__;                                                                                           \
+            }                                                                                                          \
+        }                                                                                                              \
+        else                                                                                                           \
+        {                                                                                                              \
+            using Ids = mmc::dev::GpuIds;                                                                              \
+            __VA_ARGS__;                                                                                               \
+        }                                                                                                              \
+    } while(0)
+
 namespace mmc
 {
     namespace host

@@ -327,7 +327,7 @@ namespace
         if(batched)
         {
             const uint32_t blocks = (s->slots + 7u) / 8u;
-            MMC_DISPATCH_IDS(s->handle, mmc_serve_tick_kernel<Ids><<<blocks, 256, 0, st>>>(
+            MMC_DISPATCH_IDS_SIZED(s->handle, kChunkBytes, mmc_serve_tick_kernel<Ids><<<blocks, 256, 0, st>>>(
                                             s->handle, s->d_slots, s->m_slots, s->d_chunks, s->slots, s->max_chunks,
                                             s->step, nullptr, nullptr));
         }
@@ -345,7 +345,7 @@ namespace
         mmc_serve_apply<<<8, 128, 0, st>>>(s->d_slots, s->m_slots, p.m_queue, p.m_queue_len, s->queue_cap, s->slots,
                                            &s->handle.state->error_flags);
         const uint32_t blocks = (s->slots + 7u) / 8u;
-        MMC_DISPATCH_IDS(s->handle, mmc_serve_tick_kernel<Ids><<<blocks, 256, 0, st>>>(
+        MMC_DISPATCH_IDS_SIZED(s->handle, kChunkBytes, mmc_serve_tick_kernel<Ids><<<blocks, 256, 0, st>>>(
                                         s->handle, s->d_slots, s->m_slots, s->d_chunks, s->slots, s->max_chunks,
                                         s->step, p.d_done, p.d_counts));
         mmc_status r = mmc_available_slots_async(s->heap, kChunkBytes, st, p.m_free);
@@ -599,7 +599,7 @@ mmc_status mmc_serve_tick(mmc_server* s, int batched)
                                                s->slots, &s->handle.state->error_flags);
         for(uint32_t w = 0; w < s->slots; ++w)
             if(live[w])
-                MMC_DISPATCH_IDS(s->handle, mmc_serve_one_kernel<Ids><<<1, 32, 0, stream>>>(
+                MMC_DISPATCH_IDS_SIZED(s->handle, kChunkBytes, mmc_serve_one_kernel<Ids><<<1, 32, 0, stream>>>(
                                                 s->handle, s->d_slots, s->m_slots, s->d_chunks, w, s->max_chunks,
                                                 s->step));
         st = mmc_available_slots_async(s->heap, kChunkBytes, stream, s->m_free);

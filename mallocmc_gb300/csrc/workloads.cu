@@ -67,11 +67,10 @@ constexpr uint32_t kPatternGroup = 2u; /* blocks whose read-back is in flight to
  * the 16-byte units it wrote (units lane, lane + 32, ... of every block).
  * Every lane of the warp must call it (blocks of lanes whose ptr is null are
  * skipped). Returns the pattern mismatches found in this lane's share. */
-__device__ __forceinline__ unsigned long long warp_pattern(char* ptr, uint32_t bytes, uint64_t m,
-                                                           unsigned long long& csum)
+__device__ __forceinline__ uint32_t warp_pattern(char* ptr, uint32_t bytes, uint64_t m, unsigned long long& csum)
 {
     const uint32_t lane = threadIdx.x & 31u;
-    unsigned long long bad = 0;
+    uint32_t bad = 0;
     const unsigned have = __ballot_sync(0xFFFFFFFFu, ptr != nullptr);
     for(unsigned rest = have; rest != 0u; rest &= rest - 1u)
     {
@@ -147,15 +146,19 @@ template<uint32_t PATTERN, class Ids>
 __global__ void __launch_bounds__(256, 4) mmc_stress_kernel(mmc_device_handle h, mmc_stress_params p,
                                                          const uint16_t* sizes, unsigned long long* stats)
 {
-    const uint64_t nthreads = static_cast<uint64_t>(gridDim.x) * blockDim.x;
-    const uint64_t t = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    /* 32-bit thread index and per-thread counts (a thread counts at most
+     * `rounds` pairs): at the kernel's 64-register bound every register the
+     * loop keeps live is one the allocator need not spill */
+    const uint32_t nthreads = gridDim.x * blockDim.x;
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t nsizes = (p.hi - p.lo) / p.step + 1u;
-    unsigned long long pairs = 0, nulls = 0, bad = 0, csum = 0;
+    uint32_t pairs = 0, nulls = 0, bad = 0;
+    unsigned long long csum = 0;
     for(uint32_t r = 0; r < p.rounds; ++r)
     {
         const uint64_t m = mix64(p.seed, t, r);
-        const uint32_t bytes
-            = sizes ? sizes[r * nthreads + t] : p.lo + (static_cast<uint32_t>(m >> 32) % nsizes) * p.step;
+        const uint32_t bytes = sizes ? sizes[static_cast<uint64_t>(r) * nthreads + t]
+                                     : p.lo + (static_cast<uint32_t>(m >> 32) % nsizes) * p.step;
         char* ptr = static_cast<char*>(dv::malloc<Ids>(h, bytes));
         if constexpr(PATTERN == MMC_PATTERN_WARP)
         {
@@ -203,11 +206,11 @@ __global__ void __launch_bounds__(256, 4) mmc_stress_kernel(mmc_device_handle h,
     }
     if((threadIdx.x & 31u) == 0u)
     {
-        atomicAdd(&stats[0], pairs);
+        atomicAdd(&stats[0], static_cast<unsigned long long>(pairs));
         if(nulls)
-            atomicAdd(&stats[1], nulls);
+            atomicAdd(&stats[1], static_cast<unsigned long long>(nulls));
         if(bad)
-            atomicAdd(&stats[2], bad);
+            atomicAdd(&stats[2], static_cast<unsigned long long>(bad));
         atomicXor(&stats[3], csum);
     }
 }
@@ -510,7 +513,10 @@ mmc_status mmc_run_stress(mmc_heap* heap, const mmc_stress_params* p, const uint
         return fail(MMC_ERR_ARG, "bad stress parameters");
     mmc_device_handle h;
     mmc_heap_device_handle(heap, &h);
-    /* one instantiation per pattern mode: only the mode's code is in the kernel */
+    /* One instantiation per pattern mode: only the mode's code is in the
+     * kernel. It keeps the multi-page path even when hi fits a page: built
+     * without it (SmallRequests) the uniform stress measured 1.5 % slower on
+     * GB300, from a different allocation of its 64 registers. */
     MMC_DISPATCH_IDS(h, if(p->write_pattern == MMC_PATTERN_WARP) mmc_stress_kernel<MMC_PATTERN_WARP, Ids>
                             <<<p->blocks, p->threads_per_block, 0, as_stream(stream)>>>(h, *p, sizes, stats);
                      else mmc_stress_kernel<MMC_PATTERN_THREAD, Ids>

@@ -25,6 +25,7 @@ def ex():
     L.mmcx_oldmalloc.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_ulonglong),
                                  ctypes.POINTER(ctypes.c_ulonglong), ctypes.POINTER(ctypes.c_uint),
                                  ctypes.POINTER(ctypes.c_int)]
+    L.mmcx_small_requests.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint)]
     L.mmcx_info.argtypes = [ctypes.c_char_p, ctypes.c_size_t]
     L.mmcx_policy_matrix_info.argtypes = [ctypes.c_char_p, ctypes.c_size_t]
     L.mmcx_policy_matrix_kernel.argtypes = [ctypes.c_int]
@@ -101,3 +102,18 @@ def test_oldmalloc_policy_on_cuda_device_heap(ex):
     assert fails.value == 0
     assert s.value == g.value
     assert slots.value == 0
+
+
+@pytest.mark.gpu
+def test_small_requests_kernel_has_no_multi_page_path(ex):
+    """A user kernel built with mmc::dev::SmallRequests (no multi-page search):
+    its small request is served, its request above a page fails with
+    MMC_DEVERR_PAGEBASED, and the handle's own malloc serves the same large
+    request."""
+    from mallocmc_gb300 import _lib as L
+
+    out = np.zeros(3, dtype=np.int32)
+    flags = ctypes.c_uint()
+    assert ex.mmcx_small_requests(0, out.ctypes.data, ctypes.byref(flags)) == 0
+    assert list(out) == [1, 1, 1]
+    assert flags.value == L.MMC_DEVERR_PAGEBASED
