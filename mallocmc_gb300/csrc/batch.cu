@@ -193,7 +193,10 @@ __global__ void __launch_bounds__(256, 4) mmc_batch_kernel(mmc_device_handle h, 
     float logq = 0.0f;
     mmc_job j{};
     bool done = false;
-    unsigned long long pairs = 0, nulls = 0, bad = 0, csum = 0;
+    /* 32-bit per-thread counts (a job thread runs at most max_cycles): at
+     * the kernel's 64-register bound, registers the loop need not spill */
+    uint32_t pairs = 0, nulls = 0, bad = 0;
+    unsigned long long csum = 0;
     for(;;)
     {
         bool need = !done && c == cycles;
@@ -212,18 +215,18 @@ __global__ void __launch_bounds__(256, 4) mmc_batch_kernel(mmc_device_handle h, 
                     unsigned long long* s = stats + 4ull * job;
                     if constexpr(SHARED_ROWS)
                     {
-                        atomicAdd(&s_pairs[job], static_cast<uint32_t>(pairs));
+                        atomicAdd(&s_pairs[job], pairs);
                         atomicXor(&s_csum[job], csum);
                     }
                     else
                     {
-                        atomicAdd(&s[0], pairs);
+                        atomicAdd(&s[0], static_cast<unsigned long long>(pairs));
                         atomicXor(&s[3], csum);
                     }
                     if(nulls)
-                        atomicAdd(&s[1], nulls);
+                        atomicAdd(&s[1], static_cast<unsigned long long>(nulls));
                     if(bad)
-                        atomicAdd(&s[2], bad);
+                        atomicAdd(&s[2], static_cast<unsigned long long>(bad));
                     pairs = nulls = bad = csum = 0;
                     cycles = c = 0;
                 }

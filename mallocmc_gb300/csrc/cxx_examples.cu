@@ -361,7 +361,7 @@ int mmcx_small_requests(int device, int* out, unsigned* flags)
     try
     {
         cudaSetDevice(device);
-        ScatterAllocator alloc(device, nullptr, 256U * 1024U * 1024U);
+        ScatterAllocator alloc(device, nullptr, 1U * 1024U * 1024U * 1024U);
         int* d_out = nullptr;
         cudaMalloc(&d_out, 3 * sizeof(int));
         smallRequestsKernel<<<1, 1>>>(alloc.getAllocatorHandle(), d_out);
