@@ -170,7 +170,7 @@ def batched_algorithmic_atomics(jobs, pagesize: int) -> dict:
 # a 2 GiB heap with 20 rounds (profiles/mmc_stress_kernel_uniform_2GiB_20rounds.md):
 # the partial lines at the blocks' ends (their whole lines are discarded from L2
 # before the free) and the metadata, so it scales with pairs.
-STRESS_DRAM_BYTES_PER_PAIR = 166.0
+STRESS_DRAM_BYTES_PER_PAIR = 145.0
 # L2 atomic requests per pair counted by ncu (lts__t_requests_srcunit_tex_op_atom*
 # + op_red) in the same capture: below the reference algorithm's 4.72 because a
 # formatted page's chunk size is loaded instead of CAS'd and same-size lanes
@@ -178,7 +178,7 @@ STRESS_DRAM_BYTES_PER_PAIR = 166.0
 STRESS_NCU_ATOMICS_PER_PAIR = 3.93
 # L2 atomic requests per pair of the batched workload's persistent kernel, from
 # an ncu capture on the tuned geometry (profiles/mmc_batch_kernel_512jobs_4GiB.md).
-BATCH_NCU_ATOMICS_PER_PAIR = 0.211
+BATCH_NCU_ATOMICS_PER_PAIR = 0.212
 STRESS_TRAFFIC_NOTE = ("dram__bytes_read.sum + dram__bytes_write.sum per pair from an ncu capture of the same "
                        "kernel on a 2 GiB heap / 20 rounds, times the pairs of one launch")
 
