@@ -70,6 +70,11 @@ struct mmc_server
     const uint32_t* m_queue_len;
     mmc_serve_slot* m_slots;
     unsigned* m_free;
+    /* the fused free-slot count: one sum per scan block and the count of
+     * blocks that have added theirs (zero between ticks) */
+    uint32_t count_blocks;
+    uint32_t* d_count_partials;
+    uint32_t* d_count_arrived;
     cudaStream_t stream;
     cudaGraphExec_t exec;
     cudaGraph_t graph;
@@ -266,6 +271,86 @@ __global__ void mmc_serve_publish(const mmc_serve_done* done, unsigned long long
     }
 }
 
+/* The tick's free-slot count, getAvailableSlots(slot) for a slot below the
+ * page size (the single-page branch, Scatter.hpp:1164-1193, summed over the
+ * pages as mmc_slots_pass1/2 sum it), and for a pipelined tick the
+ * publication of its results (mmc_serve_publish), in one kernel: each block
+ * sums the free slots of its page range, and the last block to add its sum
+ * (a device-scope arrival count, which that block sets back to zero for the
+ * next tick) totals the block sums, writes the count and publishes. It saves
+ * a tick two kernel boundaries over {pass 1, pass 2, publish}. No block waits
+ * for another. */
+constexpr uint32_t kCountThreads = 256;
+
+template<bool PUBLISH>
+__global__ void __launch_bounds__(kCountThreads)
+    mmc_serve_count(mmc_device_handle h, uint32_t slot, uint32_t* partials, uint32_t* arrived, unsigned* out_free,
+                    const mmc_serve_done* done, unsigned long long* counts, mmc_serve_done* out, uint32_t* out_len,
+                    unsigned long long* out_remaining)
+{
+    constexpr uint32_t nwarps = kCountThreads / 32u;
+    const uint32_t np = h.numpages;
+    const uint32_t per_block = (np + gridDim.x - 1u) / gridDim.x;
+    const uint32_t b0 = min(blockIdx.x * per_block, np);
+    const uint32_t b1 = min(b0 + per_block, np);
+    const uint32_t maxchunksize = dv::umin(h.pagesize, h.wastefactor * slot);
+    const uint32_t slotChunk = dv::umax(slot, h.paddedMinChunkSize);
+    const uint32_t capSlotChunk = dv::page_capacity(h, slotChunk);
+    uint32_t sum = 0u;
+    for(uint32_t pg = b0 + threadIdx.x; pg < b1; pg += kCountThreads)
+        sum += dv::page_free_slots(h, __ldcg(&h.chunksize[pg]), __ldcg(&h.count[pg]), slot, maxchunksize, slotChunk,
+                                   capSlotChunk);
+    __shared__ uint32_t ws[nwarps];
+    __shared__ bool last;
+    sum = __reduce_add_sync(0xFFFFFFFFu, sum);
+    if((threadIdx.x & 31u) == 0u)
+        ws[threadIdx.x >> 5] = sum;
+    __syncthreads();
+    if(threadIdx.x == 0u)
+    {
+        uint32_t t = 0u;
+        for(uint32_t w = 0; w < nwarps; ++w)
+            t += ws[w];
+        partials[blockIdx.x] = t;
+        __threadfence(); /* the block's sum is visible before its arrival is */
+        last = atomicAdd(arrived, 1u) == gridDim.x - 1u;
+    }
+    __syncthreads();
+    if(!last)
+        return;
+    __threadfence(); /* the other blocks' sums are read after their arrivals */
+    uint32_t t = 0u;
+    for(uint32_t i = threadIdx.x; i < gridDim.x; i += kCountThreads)
+        t += __ldcg(&partials[i]);
+    t = __reduce_add_sync(0xFFFFFFFFu, t);
+    __syncthreads();
+    if((threadIdx.x & 31u) == 0u)
+        ws[threadIdx.x >> 5] = t;
+    __syncthreads();
+    if(threadIdx.x == 0u)
+    {
+        uint32_t total = 0u;
+        for(uint32_t w = 0; w < nwarps; ++w)
+            total += ws[w];
+        *out_free = total;
+        *arrived = 0u; /* every block has arrived */
+    }
+    if constexpr(PUBLISH)
+    {
+        const uint32_t n = static_cast<uint32_t>(counts[0]);
+        for(uint32_t i = threadIdx.x; i < n; i += kCountThreads)
+            out[i] = done[i];
+        __syncthreads();
+        if(threadIdx.x == 0u)
+        {
+            *out_len = n;
+            *out_remaining = counts[1];
+            counts[0] = 0ull;
+            counts[1] = 0ull;
+        }
+    }
+}
+
 /* Per-request form: one warp, one slot. */
 template<class Ids>
 __global__ void mmc_serve_one_kernel(mmc_device_handle h, mmc_serve_slot* slots, mmc_serve_slot* mirror,
@@ -297,6 +382,10 @@ namespace
         cudaFreeHost(s->h_queue_len);
         cudaFreeHost(s->h_slots);
         cudaFreeHost(s->h_free);
+        if(s->d_count_partials)
+            cudaFree(s->d_count_partials);
+        if(s->d_count_arrived)
+            cudaFree(s->d_count_arrived);
         for(auto& p : s->pipe)
         {
             if(p.exec)
@@ -331,9 +420,16 @@ namespace
                                             s->handle, s->d_slots, s->m_slots, s->d_chunks, s->slots, s->max_chunks,
                                             s->step, nullptr, nullptr));
         }
-        mmc_status r = mmc_available_slots_async(s->heap, kChunkBytes, st, s->m_free);
-        if(r != MMC_OK)
-            return r;
+        if(kChunkBytes < s->handle.pagesize)
+            mmc_serve_count<false><<<s->count_blocks, kCountThreads, 0, st>>>(
+                s->handle, kChunkBytes, s->d_count_partials, s->d_count_arrived, s->m_free, nullptr, nullptr, nullptr,
+                nullptr, nullptr);
+        else
+        {
+            mmc_status r = mmc_available_slots_async(s->heap, kChunkBytes, st, s->m_free);
+            if(r != MMC_OK)
+                return r;
+        }
         return cuda_check(cudaGetLastError(), "serve tick");
     }
     /* A pipelined tick on buffer b: apply its queue, grow, count the free
@@ -348,10 +444,17 @@ namespace
         MMC_DISPATCH_IDS_SIZED(s->handle, kChunkBytes, mmc_serve_tick_kernel<Ids><<<blocks, 256, 0, st>>>(
                                         s->handle, s->d_slots, s->m_slots, s->d_chunks, s->slots, s->max_chunks,
                                         s->step, p.d_done, p.d_counts));
-        mmc_status r = mmc_available_slots_async(s->heap, kChunkBytes, st, p.m_free);
-        if(r != MMC_OK)
-            return r;
-        mmc_serve_publish<<<1, 256, 0, st>>>(p.d_done, p.d_counts, p.m_done, p.m_done_len, p.m_remaining);
+        if(kChunkBytes < s->handle.pagesize)
+            mmc_serve_count<true><<<s->count_blocks, kCountThreads, 0, st>>>(
+                s->handle, kChunkBytes, s->d_count_partials, s->d_count_arrived, p.m_free, p.d_done, p.d_counts,
+                p.m_done, p.m_done_len, p.m_remaining);
+        else
+        {
+            mmc_status r = mmc_available_slots_async(s->heap, kChunkBytes, st, p.m_free);
+            if(r != MMC_OK)
+                return r;
+            mmc_serve_publish<<<1, 256, 0, st>>>(p.d_done, p.d_counts, p.m_done, p.m_done_len, p.m_remaining);
+        }
         return cuda_check(cudaGetLastError(), "pipelined serve tick");
     }
 
@@ -415,6 +518,13 @@ mmc_status mmc_serve_create(mmc_heap* heap, uint32_t slots, uint32_t max_chunks,
     if(st == MMC_OK)
         st = cuda_check(cudaHostGetDevicePointer(reinterpret_cast<void**>(&s->m_free), s->h_free, 0),
                         "mapped free count");
+    s->count_blocks = scan_grid(s->device);
+    if(st == MMC_OK)
+        st = cuda_check(cudaMalloc(&s->d_count_partials, sizeof(uint32_t) * s->count_blocks), "count partials");
+    if(st == MMC_OK)
+        st = cuda_check(cudaMalloc(&s->d_count_arrived, sizeof(uint32_t)), "count arrivals");
+    if(st == MMC_OK)
+        st = cuda_check(cudaMemset(s->d_count_arrived, 0, sizeof(uint32_t)), "zero count arrivals");
     if(st == MMC_OK)
         st = cuda_check(cudaMemset(s->d_slots, 0, sizeof(mmc_serve_slot) * slots), "zero slots");
     if(st == MMC_OK)

@@ -42,6 +42,38 @@ def test_mix_and_alone_checksums_equal():
         assert alloc.error_flags() == 0
 
 
+def test_tick_free_count_equals_get_available_slots():
+    """A tick's free-chunk count (the fused count kernel: block sums totalled by
+    the last block to finish) equals getAvailableSlots(16 KiB) on the same heap
+    state, for the synchronous and the pipelined tick, on a heap that other
+    blocks of several sizes (formatted pages of other chunk sizes, multi-page
+    runs) partly fill; and again once they are freed."""
+    from mallocmc_gb300.serve import Server
+    from mallocmc_gb300.workloads import alloc_offsets, free_offsets
+
+    rng = np.random.default_rng(12)
+    n = 16 * 128
+    sizes = rng.choice([64, 1024, 4096, 16384, 65536, 3 * 65536], size=n).astype(np.uint32)
+    with gpu_allocator(HeapConfig(65536, 64 << 20, 16, 2, False), 512 << 20) as alloc:
+        srv = Server(alloc, slots=64, max_chunks=16, step=64, queue_cap=128)
+        ds, offs = alloc_offsets(alloc, 16, 128, sizes, 3)
+        for rep in range(2):
+            want = alloc.getAvailableSlots(16384)
+            srv.queue_len[0] = 0
+            srv.tick(batched=True)
+            srv.wait()
+            assert int(srv.free_chunks[0]) == want
+            for b in (0, 1):
+                srv._pipe[b]["qlen"][0] = 0
+                srv.launch(b)
+                srv.wait_buffer(b)
+                assert int(srv._pipe[b]["free"][0]) == want
+            if rep == 0:
+                assert free_offsets(alloc, 16, 128, ds, offs, 3) == 0
+        srv.close()
+        assert alloc.error_flags() == 0
+
+
 @pytest.mark.parametrize("pipelined", [False, True])
 def test_admission_waits_for_free_chunks(pipelined):
     """A heap too small for all requests at once: admission must hold requests
