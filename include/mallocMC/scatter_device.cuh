@@ -1166,6 +1166,8 @@ namespace mmc
                     const u32 comp = 3u - (j % 4u);
                     const u32 x = comp == 3u ? G.w : (comp == 2u ? G.z : (comp == 1u ? G.y : G.x));
                     wl = w;
+                    if(x == 0u)
+                        MMC_STAT(c, MMC_STAT_PAGE_SCAN_USED);
                     q = scan_freemap_word(x, w, w == whi ? ((top - 1u) & 31u) : 31u, w == wend ? (endpage & 31u) : 0u,
                                           n, freecount, left_free);
                     if(q != kNoRun)

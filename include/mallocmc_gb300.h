@@ -68,6 +68,7 @@ typedef enum mmc_status
 #define MMC_STAT_PAGE_SCAN 9     /* page-table words read by concurrent multi-page searches */
 #define MMC_STAT_PAGE_LOST 10    /* runs a concurrent multi-page search lost to another claim */
 #define MMC_STAT_PAGE_BASED_FAIL 11 /* concurrent multi-page allocations that returned NULL */
+#define MMC_STAT_PAGE_SCAN_USED 12 /* free-page bitmap words those searches read with no free page */
 #define MMC_STAT_COUNT 16
 
 /* Heap configuration: the template parameters of Scatter<HeapConfig, HashConfig>
