@@ -147,3 +147,42 @@ def run_fragmentation(alloc: Allocator, seed: int, blocks: int, threads_per_bloc
         c = ctr.cpu().numpy().view(np.uint64)
         out.update(released_live_bytes=int(c[1]), tag_errors=int(c[3]))
     return out
+
+
+def main(argv=None):
+    """Run the fragmentation workload once on a fresh heap (pagesize 4096,
+    regionsize 16, wastefactor 2, the fill-tuned hash distances of
+    autotune.GB300_FRAG_TUNED unless given) and print its fills, times and
+    check results as one JSON line; exit status 1 if a tag was damaged or a
+    block was not given back."""
+    import argparse
+    import json
+
+    import torch
+
+    from .autotune import GB300_FRAG_TUNED, FragConfig, frag_allocator
+
+    ap = argparse.ArgumentParser(prog="python -m mallocmc_gb300.fragmentation")
+    ap.add_argument("--heap-gib", type=float, default=32.0)
+    ap.add_argument("--accessblock-mib", type=int, default=256)
+    ap.add_argument("--seed", type=int, default=42)
+    ap.add_argument("--blocks-per-sm", type=int, default=2, help="a wave holds at most SMs x this x 256 requests")
+    ap.add_argument("--hash", default=None, help="hashingDistMP,WP,WPRel (default: the tuned distances)")
+    a = ap.parse_args(argv)
+
+    cfg = FragConfig(*[int(x) for x in a.hash.split(",")]) if a.hash else GB300_FRAG_TUNED
+    heap_bytes = int(a.heap_gib * (1 << 30))
+    sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    alloc = frag_allocator(heap_bytes, a.accessblock_mib << 20, cfg)
+    try:
+        r = run_fragmentation(alloc, a.seed, sms * a.blocks_per_sm, 256, capacity=1 << 23, release=True)
+    finally:
+        alloc.close()
+    ok = r["tag_errors"] == 0 and r["released_live_bytes"] == 0 and not r["list_overflow"]
+    keys = ("phase1_fill", "final_fill", "phase1_seconds", "phase2_seconds", "ops_per_second", "waves", "tag_errors")
+    print(json.dumps({"ok": ok, **{k: r[k] for k in keys}}))
+    return 0 if ok else 1
+
+
+if __name__ == "__main__":
+    raise SystemExit(main())
