@@ -40,6 +40,7 @@ namespace
 {
     constexpr uint32_t kChunkBytes = 16384;
     constexpr uint32_t kElemsPerChunk = 256;
+    static_assert(kElemsPerChunk * 2u == 32u * 16u, "a chunk's elements are one 16-byte load per lane of a warp");
 
     __host__ __device__ __forceinline__ uint64_t mix64(uint64_t seed, uint64_t a, uint64_t b)
     {
@@ -195,12 +196,28 @@ __device__ __forceinline__ void grow_request(const mmc_device_handle& h, mmc_ser
     __syncwarp();
     if(failed == 0u && end == s.final_len)
     {
-        /* complete: read every element back, checksum, free the chunks */
+        /* complete: read every element back, checksum, free the chunks. A
+         * chunk's 256 elements are 512 contiguous bytes (at the chunk's
+         * 16-byte aligned start), one 16-byte load per lane: the warp reads a
+         * chunk per instruction, four chunks in flight, instead of 64 bytes
+         * per instruction element by element. Bytes past the request's last
+         * element lie inside its last chunk and are not summed. */
         unsigned long long sum = 0ull;
-        for(uint32_t e = lane; e < end; e += 32u)
+        const uint32_t nch = (end + kElemsPerChunk - 1u) / kElemsPerChunk;
+#pragma unroll 4
+        for(uint32_t c = 0; c < nch; ++c)
         {
-            const uint16_t v = static_cast<const uint16_t*>(chunks[e / kElemsPerChunk])[e % kElemsPerChunk];
-            sum += static_cast<unsigned long long>(v) * (e + 1ull);
+            const uint4 v = reinterpret_cast<const uint4*>(chunks[c])[lane];
+            const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+            const uint32_t e0 = c * kElemsPerChunk + lane * 8u;
+#pragma unroll
+            for(uint32_t k = 0; k < 8u; ++k)
+            {
+                const uint32_t e = e0 + k;
+                const uint32_t x = (w[k / 2u] >> (16u * (k & 1u))) & 0xFFFFu;
+                if(e < end)
+                    sum += static_cast<unsigned long long>(x) * (e + 1ull);
+            }
         }
         for(int off = 16; off > 0; off >>= 1)
             sum += __shfl_down_sync(0xFFFFFFFFu, sum, off);
