@@ -317,3 +317,51 @@ class Server:
             if not pending.any():
                 return
         raise RuntimeError("serving loop did not drain its live requests")
+
+
+def main(argv=None):
+    """Serve one rate in one form on a fresh heap (pagesize 64 KiB; 4096 server
+    slots of up to 128 chunks, 64 elements per tick) and print one JSON line:
+    p50 / p99 admit-to-completion latency, throughput, ticks and the count of
+    wrong checksums; exit status 1 if any checksum is wrong or a request did
+    not complete."""
+    import argparse
+    import json
+
+    from .policies import AlignmentPolicies, CreationPolicies, DistributionPolicies
+
+    ap = argparse.ArgumentParser(prog="python -m mallocmc_gb300.serve")
+    ap.add_argument("--rate", type=float, default=100000.0, help="Poisson arrivals per second")
+    ap.add_argument("--seconds", type=float, default=0.5, help="arrival window (at most 50 000 requests)")
+    ap.add_argument("--heap-gib", type=int, default=64)
+    ap.add_argument("--mode", default="pipelined", choices=["pipelined", "sync", "per-request"])
+    ap.add_argument("--seed", type=int, default=None, help="request seed (default: the rate, as the bench)")
+    a = ap.parse_args(argv)
+
+    heap_bytes = a.heap_gib << 30
+    creation = CreationPolicies.Scatter(pagesize=65536, accessblocksize=min(16 << 30, heap_bytes // 2),
+                                        regionsize=16)
+    alloc = Allocator(creation, DistributionPolicies.XMallocSIMD(65536), None, None, AlignmentPolicies.Shrink(16),
+                      size=heap_bytes)
+    srv = Server(alloc, slots=4096, max_chunks=128, step=64, queue_cap=8192)
+    n = int(min(a.rate * a.seconds, 50000))
+    arrivals, lengths, seeds = make_requests(n, a.rate, seed=int(a.seed if a.seed is not None else a.rate))
+    want = np.array([expected_checksum(int(s), int(l)) for s, l in zip(seeds, lengths)], dtype=np.uint64)
+    try:
+        res = srv.run(arrivals, lengths, seeds, batched=(a.mode != "per-request"), realtime=True,
+                      max_seconds=max(5.0, 4 * a.seconds), pipelined=(a.mode == "pipelined"))
+    finally:
+        srv.close()
+        alloc.close()
+    ok = ~np.isnan(res["done"])
+    lat = (res["done"] - res["admit"])[ok] * 1e3
+    bad = int((res["checksum"][ok] != want[ok]).sum())
+    out = {"rate_per_s": a.rate, "mode": a.mode, "requests": n, "completed": int(ok.sum()), "checksum_errors": bad,
+           "p50_ms": float(np.percentile(lat, 50)) if ok.any() else None,
+           "p99_ms": float(np.percentile(lat, 99)) if ok.any() else None, "ticks": int(res.get("ticks", 0))}
+    print(json.dumps(out))
+    return 0 if bad == 0 and int(ok.sum()) == n else 1
+
+
+if __name__ == "__main__":
+    raise SystemExit(main())

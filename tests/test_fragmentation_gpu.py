@@ -99,3 +99,11 @@ def test_default_hash_keeps_tags_and_frees_everything():
         assert alloc.error_flags() == 0
         assert_all_free(alloc.snapshot())
         assert int(np.count_nonzero(alloc.snapshot()[0][:, 0] > 4096)) == 0
+
+
+def test_command_line_runs_the_workload():
+    """python -m mallocmc_gb300.fragmentation on a 1 GiB heap: the workload runs
+    to both NULLs, keeps its tags and gives every block back (exit status 0)."""
+    from mallocmc_gb300.fragmentation import main
+
+    assert main(["--heap-gib", "1"]) == 0

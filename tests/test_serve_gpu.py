@@ -177,3 +177,11 @@ def test_serving_on_a_16_gib_heap_at_a_realistic_rate():
         srv.close()
         assert_all_free(alloc.snapshot(), pagesize=65536)
         assert alloc.error_flags() == 0
+
+
+def test_command_line_serves_every_request():
+    """python -m mallocmc_gb300.serve at 2 k requests/s for 0.2 s on a 4 GiB
+    heap: every request completes with its checksum (exit status 0)."""
+    from mallocmc_gb300.serve import main
+
+    assert main(["--rate", "2000", "--seconds", "0.2", "--heap-gib", "4"]) == 0
