@@ -1307,12 +1307,15 @@ namespace mmc
          *
          * Release: every access this thread made to the block is performed
          * before the atomics that hand the block to a next owner, by a release
-         * fence ahead of them. Every lane fences before the lanes that free
-         * parts of one chunk meet at a __syncwarp, so each lane's accesses to
-         * its part are performed before the one grouped decrement. The reference's free has no such
-         * fence; without it a thread's last reads of the block can be served
-         * after a next owner's writes (a per-thread write/verify/free stress on
-         * GB300 read foreign data in 1 to 6 of 25 runs, none with the fence). */
+         * fence ahead of them; the fence is cumulative, so it also covers what
+         * other lanes of the warp did to the block before a __syncwarp this
+         * thread passed (a warp-cooperative pattern's writes and reads). Every
+         * lane fences before the lanes that free parts of one chunk meet at a
+         * __syncwarp, so each lane's accesses to its part are performed before
+         * the one grouped decrement. The reference's free has no such fence;
+         * without it a thread's last reads of the block can be served after a
+         * next owner's writes (a per-thread write/verify/free stress on GB300
+         * read foreign data in 1 to 6 of 25 runs, none with the fence). */
         template<class Ids>
         __device__ void destroy(const mmc_device_handle& h, void* mem)
         {
@@ -1479,8 +1482,9 @@ namespace mmc
          * free that follows issues a fence.release.gpu in every lane ahead of
          * the relaxed device-scope atomics that release the chunk, which
          * orders the discards (and every earlier access of the thread to the
-         * block) before those atomics: a fence followed by a strong write is
-         * a release pattern. A later owner can reach the block only
+         * block, including what other lanes of the warp wrote into it before a
+         * __syncwarp this thread passed) before those atomics: a fence followed
+         * by a strong write is a release pattern. A later owner can reach the block only
          * through an atomic that reads what those atomics wrote, and its
          * accesses to the block take their address from that atomic's result,
          * so they reach L2 after the discards. (A dependent read of each

@@ -49,7 +49,8 @@ typedef enum mmc_status
 #define MMC_DEVERR_TIMEOUT 0x1u  /* the page-based mutex wait hit its iteration bound */
 #define MMC_DEVERR_BADFREE 0x2u  /* free of a pointer outside the heap or on an unformatted page */
 #define MMC_DEVERR_OOM 0x4u      /* an allocation failed under MMC_OOM_FLAG */
-#define MMC_DEVERR_BADCMD 0x8u   /* a serving tick skipped a command (slot beyond the table, unknown kind)
+#define MMC_DEVERR_BADCMD 0x8u   /* a serving tick skipped a command (slot beyond the table, unknown kind,
+                                    an admission longer than a slot's chunks hold)
                                     or cut a queue length beyond the queue's capacity */
 #define MMC_DEVERR_PAGEBASED 0x10u /* a request above a page in a kernel built without the multi-page path
                                       (mmc::dev::SmallRequests: a batch whose job sizes fit a page, for one) */
@@ -270,7 +271,8 @@ mmc_status mmc_run_program(mmc_heap* heap, const uint8_t* kinds, const uint64_t*
  * verify it, free}). Sizes: sizes[r * T + t] (u16, bytes; T = blocks x
  * threads_per_block) if sizes != NULL, else drawn from seed uniformly in
  * {lo, lo+step, ..., hi}. stats (device, 4 x u64, accumulated, caller zeroes):
- * {pairs, nulls, pattern errors, checksum}. */
+ * {pairs, nulls, pattern errors, checksum}. At most 2^32 threads and 2^26
+ * rounds (MMC_ERR_ARG otherwise). */
 typedef struct mmc_stress_params
 {
     uint32_t blocks;
@@ -432,10 +434,12 @@ mmc_status mmc_serve_queue(mmc_server* server, mmc_serve_cmd** queue, uint32_t**
                            unsigned** free_chunks);
 /* Run one tick and wait for it: batched != 0 replays the captured graph (all
  * live requests in one launch); 0 launches one kernel per live request. The
- * queue is checked first (mmc_serve_check_queue): on MMC_ERR_ARG nothing is
- * launched. The tick's kernels check it again, since the queue is host memory
- * the caller may change at any time: they cut a length beyond the capacity and
- * skip a bad command, and set MMC_DEVERR_BADCMD (mmc_heap_error). */
+ * queue is checked first (mmc_serve_check_queue, and every admission's
+ * final_len against the max_chunks x 256 elements a slot holds): on
+ * MMC_ERR_ARG nothing is launched. The tick's kernels check it again, since
+ * the queue is host memory the caller may change at any time: they cut a
+ * length beyond the capacity and skip a bad command, and set
+ * MMC_DEVERR_BADCMD (mmc_heap_error). */
 mmc_status mmc_serve_tick(mmc_server* server, int batched);
 
 /* Host-side check of a command queue before a tick: MMC_ERR_ARG when

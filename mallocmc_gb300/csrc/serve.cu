@@ -109,10 +109,12 @@ struct mmc_server
  * host's queue; each changed slot is also written to the host's table. The
  * queue lives in host-written memory, so nothing in it is trusted: a length
  * beyond the queue's capacity is cut to it, and a command naming a slot
- * beyond the table or an unknown kind is skipped; either sets
- * MMC_DEVERR_BADCMD in the heap's error word. */
+ * beyond the table, an unknown kind or an admission longer than a slot's
+ * chunks hold (max_len elements) is skipped; either sets MMC_DEVERR_BADCMD in
+ * the heap's error word. */
 __global__ void mmc_serve_apply(mmc_serve_slot* slots, mmc_serve_slot* mirror, const mmc_serve_cmd* q,
-                                const uint32_t* qlen, uint32_t queue_cap, uint32_t nslots, uint32_t* error_flags)
+                                const uint32_t* qlen, uint32_t queue_cap, uint32_t nslots, uint32_t max_len,
+                                uint32_t* error_flags)
 {
     uint32_t n = *qlen;
     if(n > queue_cap)
@@ -124,7 +126,7 @@ __global__ void mmc_serve_apply(mmc_serve_slot* slots, mmc_serve_slot* mirror, c
     for(uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
     {
         const mmc_serve_cmd c = q[i];
-        if(c.slot >= nslots || (c.kind != 1u && c.kind != 2u))
+        if(c.slot >= nslots || (c.kind != 1u && c.kind != 2u) || (c.kind == 1u && c.final_len > max_len))
         {
             atomicOr(error_flags, MMC_DEVERR_BADCMD);
             continue;
@@ -423,13 +425,33 @@ namespace
         delete s;
     }
 
+    /* The longest request a slot can hold: its chunk row's elements. */
+    uint32_t max_request_len(const mmc_server* s)
+    {
+        const uint64_t n = static_cast<uint64_t>(s->max_chunks) * kElemsPerChunk;
+        return n > 0xFFFFFFFFull ? 0xFFFFFFFFu : static_cast<uint32_t>(n);
+    }
+
+    /* An admission longer than a slot's chunks hold would index past its row
+     * of the chunk table: refused before a tick is launched. */
+    mmc_status check_admission_lengths(const mmc_server* s, const mmc_serve_cmd* q, uint32_t n)
+    {
+        const uint32_t max_len = max_request_len(s);
+        for(uint32_t i = 0; i < n; ++i)
+            if(q[i].kind == 1u && q[i].final_len > max_len)
+                return fail(MMC_ERR_ARG, "command " + std::to_string(i) + " admits " + std::to_string(q[i].final_len)
+                                             + " elements; a slot's " + std::to_string(s->max_chunks)
+                                             + " chunks hold " + std::to_string(max_len));
+        return MMC_OK;
+    }
+
     /* The tick's stream work: queue upload, apply, grow (batched) or not,
      * free-slot count, slot table and count download. */
     mmc_status enqueue_tick(mmc_server* s, bool batched)
     {
         cudaStream_t st = s->stream;
         mmc_serve_apply<<<8, 128, 0, st>>>(s->d_slots, s->m_slots, s->m_queue, s->m_queue_len, s->queue_cap, s->slots,
-                                           &s->handle.state->error_flags);
+                                           max_request_len(s), &s->handle.state->error_flags);
         if(batched)
         {
             const uint32_t blocks = (s->slots + 7u) / 8u;
@@ -456,7 +478,7 @@ namespace
         cudaStream_t st = s->stream;
         mmc_server::Pipe& p = s->pipe[b];
         mmc_serve_apply<<<8, 128, 0, st>>>(s->d_slots, s->m_slots, p.m_queue, p.m_queue_len, s->queue_cap, s->slots,
-                                           &s->handle.state->error_flags);
+                                           max_request_len(s), &s->handle.state->error_flags);
         const uint32_t blocks = (s->slots + 7u) / 8u;
         MMC_DISPATCH_IDS_SIZED(s->handle, kChunkBytes, mmc_serve_tick_kernel<Ids><<<blocks, 256, 0, st>>>(
                                         s->handle, s->d_slots, s->m_slots, s->d_chunks, s->slots, s->max_chunks,
@@ -662,6 +684,8 @@ mmc_status mmc_serve_launch(mmc_server* s, int buffer)
     /* the tick on this buffer reads the queue the host has just written: check it first */
     mmc_status q = mmc_serve_check_queue(s->pipe[buffer].h_queue, *s->pipe[buffer].h_queue_len, s->queue_cap,
                                          s->slots);
+    if(q == MMC_OK)
+        q = check_admission_lengths(s, s->pipe[buffer].h_queue, *s->pipe[buffer].h_queue_len);
     if(q != MMC_OK)
         return q;
     mmc_status st = cuda_check(cudaGraphLaunch(s->pipe[buffer].exec, s->stream), "pipelined tick launch");
@@ -706,6 +730,8 @@ mmc_status mmc_serve_tick(mmc_server* s, int batched)
     if(s == nullptr)
         return fail(MMC_ERR_ARG, "server is null");
     mmc_status st = mmc_serve_check_queue(s->h_queue, *s->h_queue_len, s->queue_cap, s->slots);
+    if(st == MMC_OK)
+        st = check_admission_lengths(s, s->h_queue, *s->h_queue_len);
     if(st != MMC_OK)
         return st;
     if(batched)
@@ -723,7 +749,7 @@ mmc_status mmc_serve_tick(mmc_server* s, int batched)
         for(uint32_t i = 0; i < *s->h_queue_len; ++i)
             live[s->h_queue[i].slot] = s->h_queue[i].kind == 1u;
         mmc_serve_apply<<<8, 128, 0, stream>>>(s->d_slots, s->m_slots, s->m_queue, s->m_queue_len, s->queue_cap,
-                                               s->slots, &s->handle.state->error_flags);
+                                               s->slots, max_request_len(s), &s->handle.state->error_flags);
         for(uint32_t w = 0; w < s->slots; ++w)
             if(live[w])
                 MMC_DISPATCH_IDS_SIZED(s->handle, kChunkBytes, mmc_serve_one_kernel<Ids><<<1, 32, 0, stream>>>(

@@ -511,6 +511,9 @@ mmc_status mmc_run_stress(mmc_heap* heap, const mmc_stress_params* p, const uint
        || p->hi < p->lo || (p->write_pattern != MMC_PATTERN_THREAD && p->write_pattern != MMC_PATTERN_WARP)
        || (p->write_pattern == MMC_PATTERN_WARP && (p->threads_per_block % 32u) != 0u))
         return fail(MMC_ERR_ARG, "bad stress parameters");
+    /* the kernel counts threads and each warp's pairs in 32 bits */
+    if(static_cast<uint64_t>(p->blocks) * p->threads_per_block > 0xFFFFFFFFull || p->rounds > (1u << 26))
+        return fail(MMC_ERR_ARG, "stress grid above 2^32 threads or more than 2^26 rounds");
     mmc_device_handle h;
     mmc_heap_device_handle(heap, &h);
     /* One instantiation per pattern mode: only the mode's code is in the

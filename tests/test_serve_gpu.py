@@ -116,7 +116,8 @@ def test_cut_short_run_drains_before_the_next():
 
 def test_tick_refuses_a_bad_queue():
     """A tick whose host-written queue is out of range (length beyond the
-    queue's capacity, a slot beyond the table, an unknown kind) is refused
+    queue's capacity, a slot beyond the table, an unknown kind, an admission
+    longer than a slot's chunks hold) is refused
     with MMC_ERR_ARG before anything is launched, in the synchronous and the
     pipelined form; a valid queue then ticks normally."""
     from mallocmc_gb300 import _lib as L
@@ -133,10 +134,14 @@ def test_tick_refuses_a_bad_queue():
             assert lib.mmc_serve_tick(srv._s, batched) == L.MMC_ERR_ARG
             srv.queue[0] = (3, 0, 0, 100, 1)
             assert lib.mmc_serve_tick(srv._s, batched) == L.MMC_ERR_ARG
+            srv.queue[0] = (1, 0, 0, 16 * 256 + 1, 1)  # longer than the slot's 16 chunks hold
+            assert lib.mmc_serve_tick(srv._s, batched) == L.MMC_ERR_ARG
         pq = srv._pipe[0]["q"]
         pql = srv._pipe[0]["qlen"]
         pql[0] = 1
         pq["kind"][0], pq["slot"][0] = 1, 9
+        assert lib.mmc_serve_launch(srv._s, 0) == L.MMC_ERR_ARG
+        pq["slot"][0], pq["final_len"][0] = 1, 16 * 256 + 1
         assert lib.mmc_serve_launch(srv._s, 0) == L.MMC_ERR_ARG
         pql[0] = 0
         srv.queue[0] = (1, 2, 0, 100, 1)
